@@ -1,0 +1,168 @@
+/*
+ * uhs.h -- C ABI of the GB300 stencil backend for UHStencil.
+ *
+ * The backend replaces what UHStencil's GPU lowering produces for one stencil
+ * program: the generated sweep kernel (one stencil.apply over the domain) and
+ * the generated program entry _mlir_ciface_<name>_iteration that runs T/2
+ * ping-pong pairs of sweeps.  Callers hand in device memory exactly as the
+ * reference's drivers do (UH-GPU/3d1r_star/3d7pt_main.cpp:117-150): two
+ * caller-allocated grids described by MLIR memref descriptors, result in the
+ * first one.  Everything here is plain C: pointers, sizes, status codes.
+ *
+ * Grid layout: row-major, slowest axis first, unit stride on the fastest axis,
+ * halo cells included in the extents (a 512^3 interior with a 1-cell halo is
+ * a 514^3 memref).  A rank-2 grid is passed as rank 3 with sizes[0] == 1.
+ *
+ * Status: every entry returns an int status; uhs_last_error() gives the
+ * message of the last failing call on the calling thread.
+ */
+#ifndef UHS_H_
+#define UHS_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define UHS_ABI_VERSION 1
+
+/* Largest expression the sweep kernels accept: 343 terms (7^3 box) plus room
+ * for hand-written programs. */
+#define UHS_MAX_TERMS 512
+/* Largest |offset| on any axis. */
+#define UHS_MAX_RADIUS 4
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    UHS_OK = 0,
+    UHS_EINVAL = 1,       /* malformed descriptor, memref or parameters */
+    UHS_EUNSUPPORTED = 2, /* well-formed but outside what the kernels cover */
+    UHS_ECUDA = 3,        /* a CUDA call failed; the message names it */
+    UHS_ETIMEOUT = 4,     /* a device-side wait ran out of its bound */
+    UHS_ENOMEM = 5,       /* a runtime-owned allocation failed */
+    UHS_ERANGE = 6,       /* a value is outside what the chosen arithmetic represents */
+    UHS_EPARSE = 7        /* DSL text did not parse */
+};
+
+/* ---- element types and arithmetic -------------------------------------- */
+enum {
+    UHS_F64 = 0,  /* double grids (the reference's type in every case) */
+    UHS_F32 = 1,  /* float grids, float arithmetic */
+    UHS_F32X2 = 2 /* compensated pair: two float grids, value = hi + lo */
+};
+
+enum {
+    UHS_ARITH_AUTO = 0,  /* the backend picks (fastest mode within 1e-12 for F64) */
+    UHS_ARITH_FMA = 1,   /* native arithmetic, products fused into the sum */
+    UHS_ARITH_EXACT = 2, /* separately rounded products and sums in expression
+                            order: bit-identical to the serial CPU loops */
+    UHS_ARITH_DF32 = 3   /* F64 grids computed in float-pair (~48-bit) arithmetic
+                            on the FP32 pipes; results within 1e-12 of FP64 */
+};
+
+/* ---- MLIR memref descriptor (rank-3 layout) ---------------------------- */
+/* Same field order as MLIR's StridedMemRefType<T, 3>; strides and offset
+ * count elements.  The element address of (z, y, x) is
+ *   aligned + offset + z*strides[0] + y*strides[1] + x*strides[2]. */
+typedef struct uhs_memref {
+    void *allocated;
+    void *aligned;
+    int64_t offset;
+    int64_t sizes[3];
+    int64_t strides[3];
+} uhs_memref;
+
+/* ---- stencil descriptor ------------------------------------------------ */
+/* One term of the linear form  out[p] = sum_k coef_k * in[p + (dz,dy,dx)_k].
+ * Terms are kept in the order the .dsl expression writes them.  A term whose
+ * param >= 0 takes its coefficient from the parameter array of the program
+ * (the DSL's `c[2]*U[x-1]...` form); coef is ignored for it. */
+typedef struct uhs_term {
+    int32_t dz, dy, dx;
+    int32_t param;
+    double coef;
+} uhs_term;
+
+typedef struct uhs_stencil_desc {
+    int32_t rank;         /* 2 or 3 */
+    int32_t dtype;        /* UHS_F64 / UHS_F32 / UHS_F32X2 */
+    int64_t lb[3];        /* domain, slowest first; rank 2: lb[0]=0, ub[0]=1 */
+    int64_t ub[3];
+    int32_t nterms;
+    const uhs_term *terms;
+    int32_t iterations;   /* T: 1 (single sweep a -> b) or even (T/2 pairs, result in a) */
+    const double *params; /* host copy of the parameter array, or NULL */
+    int32_t nparams;
+} uhs_stencil_desc;
+
+/* ---- tuning parameters ------------------------------------------------- */
+/* The launch parameters UHStencil fixes at compile time through pass options
+ * (tile_sizes_l0/l1, inner_tile, use smem: include/Conversion/UHAffineToParallel/
+ * Passes.td:6-101) become run-time values.  Zero means "let the backend choose"
+ * (its tuner database, then the learned cost model, then defaults). */
+enum {
+    UHS_KERNEL_AUTO = 0,
+    UHS_KERNEL_GENERIC = 1, /* any term list, smem plane ring, expression order */
+    UHS_KERNEL_STREAM = 2,  /* 2.5D register streaming, templated star/box shapes */
+    UHS_KERNEL_MMA = 3      /* box radius 2/3: contraction on tensor cores */
+};
+
+typedef struct uhs_params {
+    int32_t kernel;       /* UHS_KERNEL_* */
+    int32_t arith;        /* UHS_ARITH_* */
+    int32_t tile_x;       /* CTA tile along x (fastest axis) */
+    int32_t tile_y;       /* CTA tile along y */
+    int32_t tile_z;       /* planes streamed per CTA along the slowest axis (0 = all) */
+    int32_t k_temporal;   /* timesteps fused per pass over HBM */
+    int32_t use_tma;      /* -1 off, 0 auto, 1 on */
+    int32_t flags;        /* UHS_FLAG_* */
+} uhs_params;
+
+enum {
+    UHS_FLAG_NO_SYNC = 1,    /* return without synchronising the stream */
+    UHS_FLAG_NO_TUNE_DB = 2  /* ignore the tuner database for this call */
+};
+
+/* ---- entry points ------------------------------------------------------ */
+
+/* Thread-local message for the last failing call (never NULL). */
+const char *uhs_last_error(void);
+
+/* Version of this ABI (UHS_ABI_VERSION). */
+int uhs_abi_version(void);
+
+/* Fill *p with the defaults (all zero / auto). */
+void uhs_params_default(uhs_params *p);
+
+/* Check a descriptor and its two grids without touching the GPU. */
+int uhs_validate(const uhs_stencil_desc *desc, const uhs_memref *a, const uhs_memref *b);
+
+/* Run the program: desc->iterations == 1 sweeps a -> b; an even count runs
+ * iterations/2 pairs (a -> b, b -> a), leaving step T in a and step T-1 in b,
+ * like the reference's generated <name>_iteration
+ * (UHStencil/lib/Conversion/StencilToStandard/ConvertStencilToStandard.cpp:298-337).
+ * a and b are device grids of identical shape; cells outside the domain are
+ * read, never written, in both.  stream is a cudaStream_t (NULL = legacy
+ * default stream).  Unless UHS_FLAG_NO_SYNC is set the call returns after the
+ * stream has drained, which is what the reference's entry does. */
+int uhs_run(const uhs_stencil_desc *desc, const uhs_memref *a, const uhs_memref *b,
+            const uhs_params *params, void *stream);
+
+/* One sweep in -> out (the compute function MLIRGen emits beside the
+ * iteration entry, UHStencil/lib/Parser/MLIRGen.cpp:183-273). */
+int uhs_sweep(const uhs_stencil_desc *desc, const uhs_memref *in, const uhs_memref *out,
+              const uhs_params *params, void *stream);
+
+/* Pass plan the backend would use: fills kernel/arith/tiles/k of *out. */
+int uhs_plan(const uhs_stencil_desc *desc, const uhs_memref *a, const uhs_params *params,
+             uhs_params *out);
+
+/* Number of kernels this library launched since load (diagnostics). */
+int64_t uhs_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* UHS_H_ */

@@ -1,0 +1,100 @@
+"""Compile the reference's own serial stencil drivers into oracle/_ref/.
+
+TEST INFRASTRUCTURE ONLY.  The shared objects made here are the reference
+implementation that the C oracle (oracle/uhs_oracle.c) is pinned against; the
+library never loads them.
+
+Each UHStencil case directory holds a self-contained C (UH-SW) or C++ (UH-GPU)
+driver whose CPU loop (mpe_verify / cpu_verify) is the reference CPU path.  The
+drivers are compiled unmodified, straight from where they lie in the
+reference checkout, with:
+  * oracle/shim/athread.h standing in for the Sunway runtime header, and
+    oracle/shim/gpu/cuda*.h declaring the few CUDA calls of the GPU drivers'
+    main() (the installed CUDA headers changed cuCtxCreate's arguments),
+  * -Dmain=uhs_ref_unused_main so the driver's main() is never run,
+  * a generated stub file that defines every symbol the driver leaves
+    undefined outside libc (the device entry point, the CUDA calls of the GPU
+    drivers' main()); none of them is ever called.
+Flags: gcc/g++ -O2 -ffp-contract=off, the same as the oracle.
+
+Usage: python oracle/build_ref.py [REFERENCE_ROOT]
+Nothing is built when the reference checkout is absent.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+SHIM = os.path.join(HERE, "shim")
+
+# case -> (UH-SW driver, UH-GPU driver), paths relative to the reference root
+CASES = {
+    "2d1r_star": ("UH-SW/2d1r_star/stencil_2d5pt_driver.serial.c", "UH-GPU/2d1r_star/2d5pt_main.cpp"),
+    "2d2r_star": ("UH-SW/2d2r_star/stencil_2d9pt_driver.serial.c", "UH-GPU/2d2r_star/2d9pt_main.cpp"),
+    "2d3r_star": ("UH-SW/2d3r_star/stencil_2d13pt_driver.serial.c", "UH-GPU/2d3r_star/2d3r_main.cpp"),
+    "2d1r_box": ("UH-SW/2d1r_box/stencil_2d9pt_driver.serial.c", "UH-GPU/2d1r_box/2d9pt_main.cpp"),
+    "2d2r_box": ("UH-SW/2d2r_box/stencil_2d25pt_driver.serial.c", "UH-GPU/2d2r_box/2d25pt_main.cpp"),
+    "2d3r_box": ("UH-SW/2d3r_box/stencil_2d49pt_driver.serial.c", "UH-GPU/2d3r_box/2d3r_main.cpp"),
+    "3d1r_star": ("UH-SW/3d1r_star/stencil_3d7pt_driver.serial.c", "UH-GPU/3d1r_star/3d7pt_main.cpp"),
+    "3d2r_star": ("UH-SW/3d2r_star/stencil_3d13pt_driver.serial.c", "UH-GPU/3d2r_star/3d13pt_main.cpp"),
+    "3d3r_star": ("UH-SW/3d3r_star/stencil_3d19pt_driver.serial.c", "UH-GPU/3d3r_star/3d3r_main.cpp"),
+    "3d1r_box": ("UH-SW/3d1r_box/stencil_3d27pt_driver.serial.c", "UH-GPU/3d1r_box/3d27pt_main.cpp"),
+    "3d2r_box": ("UH-SW/3d2r_box/stencil_3d125pt_driver.serial.c", "UH-GPU/3d2r_box/3d125pt_main.cpp"),
+    "3d3r_box": ("UH-SW/3d3r_box/stencil_3d343pt_driver.serial.c", "UH-GPU/3d3r_box/3d3r_main.cpp"),
+}
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+
+
+def _undefined(obj: str) -> list[str]:
+    r = subprocess.run(["nm", "-u", obj], capture_output=True, text=True, check=True)
+    syms = []
+    for line in r.stdout.splitlines():
+        name = line.split()[-1].split("@")[0]
+        if name.startswith(("cu", "_mlir_ciface_", "stencil_", "athread")):
+            syms.append(name)
+    return syms
+
+
+def _build_one(ref_root: str, tag: str, src_rel: str) -> str:
+    src = os.path.join(ref_root, src_rel)
+    is_cpp = src.endswith(".cpp")
+    obj = os.path.join(OUT, f"{tag}.o")
+    so = os.path.join(OUT, f"{tag}.so")
+    stub_c = os.path.join(OUT, f"{tag}_stub.c")
+    comp = ["g++" if is_cpp else "gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-w",
+            "-Dmain=uhs_ref_unused_main", f"-I{SHIM}"]
+    if is_cpp:
+        comp += [f"-I{os.path.join(SHIM, 'gpu')}"]
+    _run(comp + ["-c", src, "-o", obj])
+    with open(stub_c, "w") as f:
+        f.write("/* generated: never-called definitions for symbols the driver leaves undefined */\n")
+        for s in _undefined(obj):
+            f.write(f"void {s}(void) {{}}\n")
+    _run(["gcc", "-O2", "-fPIC", "-shared", "-o", so, obj, stub_c] + (["-lstdc++"] if is_cpp else []))
+    return so
+
+
+def build(ref_root: str = "/root/reference") -> list[str]:
+    if not os.path.isdir(os.path.join(ref_root, "UH-SW")):
+        return []
+    os.makedirs(OUT, exist_ok=True)
+    jobs = []
+    for case, (sw, gpu) in CASES.items():
+        jobs.append((f"sw_{case}", sw))
+        jobs.append((f"gpu_{case}", gpu))
+    with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
+        return list(ex.map(lambda j: _build_one(ref_root, *j), jobs))
+
+
+if __name__ == "__main__":
+    built = build(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    print(f"built {len(built)} reference drivers into {OUT}")

@@ -1,0 +1,52 @@
+// Internal interface between the host runtime (uhs_runtime.cpp) and the sweep
+// kernels (*.cu).  Not part of the C ABI.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "../../include/uhs.h"
+
+namespace uhs {
+
+// One grid as the kernels see it: element pointer of (0,0,0), element strides.
+struct GridView {
+    void *data;
+    int64_t n[3];   // sizes, slowest first
+    int64_t s[3];   // strides in elements (s[2] == 1)
+};
+
+// A stencil program reduced to what a sweep needs.
+struct SweepSpec {
+    int rank;
+    int dtype;
+    int64_t lb[3], ub[3];
+    int nterms;
+    int32_t dz[UHS_MAX_TERMS], dy[UHS_MAX_TERMS], dx[UHS_MAX_TERMS];
+    double coef[UHS_MAX_TERMS];
+    int rz, ry, rx;        // max |offset| per axis
+    int shape;             // kShapeGeneric / kShapeStar / kShapeBox
+    int radius;            // for star/box
+};
+
+enum { kShapeGeneric = 0, kShapeStar = 1, kShapeBox = 2 };
+
+struct LaunchCfg {
+    int kernel;      // UHS_KERNEL_*
+    int arith;       // UHS_ARITH_*
+    int tile_x, tile_y, tile_z;
+    int k_temporal;
+    int use_tma;
+};
+
+// Device-side error word written by kernels that detect a problem (range
+// overflow in float-pair arithmetic, a bounded wait that ran out).
+enum : unsigned { kDevErrRange = 1u, kDevErrTimeout = 2u };
+unsigned *device_error_word(int device);
+
+// Generic smem plane-ring sweep: any term list, expression order.
+cudaError_t launch_generic(const SweepSpec &sp, const LaunchCfg &cfg, const GridView &in,
+                           const GridView &out, cudaStream_t st);
+
+// Launch counter shared by every launcher.
+void count_launch(int n = 1);
+
+}  // namespace uhs

@@ -1,0 +1,116 @@
+"""Calling the C ABI on device grids.
+
+Grids are torch CUDA tensors (torch is used for device memory and streams
+only) or raw device pointers.  Each call builds the MLIR memref descriptors the
+reference's drivers build (UH-GPU/3d1r_star/3d7pt_main.cpp:147-148) and goes
+through uhs_run / uhs_sweep.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+from . import _lib
+from .stencil import Stencil
+
+
+@dataclass
+class RunParams:
+    kernel: int = 0
+    arith: int = 0
+    tile_x: int = 0
+    tile_y: int = 0
+    tile_z: int = 0
+    k_temporal: int = 0
+    use_tma: int = 0
+    flags: int = 0
+
+    def to_c(self) -> _lib.Params:
+        return _lib.Params(self.kernel, self.arith, self.tile_x, self.tile_y, self.tile_z, self.k_temporal,
+                           self.use_tma, self.flags)
+
+    @staticmethod
+    def from_c(p: _lib.Params) -> "RunParams":
+        return RunParams(p.kernel, p.arith, p.tile_x, p.tile_y, p.tile_z, p.k_temporal, p.use_tma, p.flags)
+
+
+def memref_of(t, rank: int | None = None) -> _lib.Memref:
+    """Memref descriptor of a contiguous-in-x torch tensor of rank 2 or 3."""
+    shape = list(t.shape)
+    strides = list(t.stride())
+    if len(shape) == 2:
+        shape = [1] + shape
+        strides = [shape[1] * strides[0]] + strides
+    if len(shape) != 3:
+        raise ValueError("grids are rank-2 or rank-3 tensors")
+    m = _lib.Memref()
+    m.allocated = t.data_ptr()
+    m.aligned = t.data_ptr()
+    m.offset = 0
+    for i in range(3):
+        m.sizes[i] = shape[i]
+        m.strides[i] = strides[i]
+    return m
+
+
+def memref_raw(ptr: int, sizes, strides=None) -> _lib.Memref:
+    sizes = list(sizes)
+    if strides is None:
+        strides = [sizes[1] * sizes[2], sizes[2], 1]
+    m = _lib.Memref()
+    m.allocated = ptr
+    m.aligned = ptr
+    m.offset = 0
+    for i in range(3):
+        m.sizes[i] = sizes[i]
+        m.strides[i] = strides[i]
+    return m
+
+
+def _stream_handle(stream) -> int | None:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream  # torch.cuda.Stream
+
+
+def run(stencil: Stencil, a, b, params: RunParams | None = None, stream=None) -> None:
+    """Run the program (T = stencil.iterations) on device grids a and b."""
+    d = stencil.to_desc()
+    ma = a if isinstance(a, _lib.Memref) else memref_of(a)
+    mb = b if isinstance(b, _lib.Memref) else memref_of(b)
+    p = (params or RunParams()).to_c()
+    _lib.check(_lib.lib().uhs_run(d.ref(), ctypes.byref(ma), ctypes.byref(mb), ctypes.byref(p),
+                                  _stream_handle(stream)))
+
+
+def sweep(stencil: Stencil, src, dst, params: RunParams | None = None, stream=None) -> None:
+    """One sweep src -> dst."""
+    d = stencil.to_desc()
+    ma = src if isinstance(src, _lib.Memref) else memref_of(src)
+    mb = dst if isinstance(dst, _lib.Memref) else memref_of(dst)
+    p = (params or RunParams()).to_c()
+    _lib.check(_lib.lib().uhs_sweep(d.ref(), ctypes.byref(ma), ctypes.byref(mb), ctypes.byref(p),
+                                    _stream_handle(stream)))
+
+
+def plan(stencil: Stencil, a=None, params: RunParams | None = None) -> RunParams:
+    d = stencil.to_desc()
+    out = _lib.Params()
+    p = (params or RunParams()).to_c()
+    ma = memref_of(a) if a is not None else None
+    _lib.check(_lib.lib().uhs_plan(d.ref(), ctypes.byref(ma) if ma is not None else None, ctypes.byref(p),
+                                   ctypes.byref(out)))
+    return RunParams.from_c(out)
+
+
+def validate(stencil: Stencil, a, b) -> None:
+    d = stencil.to_desc()
+    ma = a if isinstance(a, _lib.Memref) else memref_of(a)
+    mb = b if isinstance(b, _lib.Memref) else memref_of(b)
+    _lib.check(_lib.lib().uhs_validate(d.ref(), ctypes.byref(ma), ctypes.byref(mb)))
+
+
+def launch_count() -> int:
+    return int(_lib.lib().uhs_launch_count())
