@@ -1,0 +1,335 @@
+"""Benchmark of the stencil backend on one GB300 (or N independent replicas).
+
+Workload (default): 3d1r_star (7-point) FP64 on a 512^3 interior with a
+1-cell zero halo, U[-1,1) data, 7 normalised U[0,1) coefficients, T = 50
+sweeps with double-buffer ping-pong -- the configuration the GStencil/s metric
+is quoted on.  One "step" is one complete program run (T sweeps of the grid)
+through uhs_run().
+
+Reported (one JSON line, rank 0):
+  value      GStencil/s = interior points * T / time, grids resident in HBM
+  e2e        the same metric through the C ABI with host buffers: pinned host
+             -> device copy of the input grid, the run, device -> host copy of
+             the result, all inside the timed region
+  roofline   the sweep kernel's algorithmic bytes (16 B per point-update for
+             FP64: one read and one write) per launch over its average launch
+             time, against the measured HBM copy bandwidth
+  cpu_baseline  the oracle's restatement of the reference's serial loops on
+             this host's cores, on a bounded sample of the same workload
+  fp32       the same workload on FP32 grids, with its L2 error against the
+             FP64 oracle (the north-star's FP32-vs-FP64 comparison)
+Inputs (1.09 GB per grid) are larger than the 129 MB L2, so no flush is
+needed between timed iterations.
+
+--impl reference times the reference's CPU implementation of the path (the
+oracle port of mpe_verify, all host threads) on the same workload instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg4"])
+    p.add_argument("--n", type=int, default=0, help="interior side override (smaller case for profiling)")
+    p.add_argument("--iters", type=int, default=0, help="T override")
+    p.add_argument("--arith", type=int, default=0)
+    p.add_argument("--kernel", type=int, default=0)
+    p.add_argument("--no-cpu", action="store_true", help="skip the oracle (profiling runs)")
+    p.add_argument("--no-fp32", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_workload(args):
+    from uxxxxxxxxh_gb300 import workloads as W
+    fn = getattr(W, args.config)
+    kw = {}
+    if args.n:
+        kw["n"] = args.n
+    if args.iters:
+        kw["T"] = args.iters
+    return fn(**kw)
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            if len(r) >= 9:
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip() == "Active":
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def cpu_sample(st, a0, budget_s: float = 12.0):
+    """Oracle (port of the reference's serial loops) on all host threads:
+    whole-grid sweeps, as many as fit the time budget (at most T)."""
+    import oracle
+    a, b = a0.copy(), a0.copy()
+    t0 = time.perf_counter()
+    oracle.sweep_f64(st, a, b)
+    t1 = time.perf_counter() - t0
+    sweeps = int(max(1, min(st.iterations, budget_s // max(t1, 1e-6))))
+    if sweeps > 1:
+        t0 = time.perf_counter()
+        for i in range(sweeps):
+            if i % 2 == 0:
+                oracle.sweep_f64(st, a, b)
+            else:
+                oracle.sweep_f64(st, b, a)
+        t1 = time.perf_counter() - t0
+    gst = st.interior_points * sweeps / t1 / 1e9
+    return {"value": gst, "unit": "GStencil/s", "cores": oracle.max_threads(), "kind": "port",
+            "sample": f"{sweeps} whole-grid sweep(s) of the {st.name} grid {tuple(st.sizes)} "
+                      f"({st.interior_points} interior points each)", "seconds": t1}
+
+
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    import oracle
+    st, a0 = make_workload(args)
+    oracle.set_threads(os.cpu_count() or 1)
+    for _ in range(args.warmup):
+        cpu_sample(st, a0, budget_s=1.0)
+    vals = []
+    samp = None
+    for _ in range(args.steps):
+        samp = cpu_sample(st, a0, budget_s=8.0)
+        vals.append(samp["value"])
+    v = statistics.median(vals)
+    samp["value"] = v
+    line = {"metric": "GStencil/s", "value": v, "unit": "GStencil/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": samp["seconds"] * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
+            "impl": "reference",
+            "config": {"workload": f"{st.name} {st.interior_points ** (1 / st.rank):.0f}^{st.rank} T={st.iterations}",
+                       "l2": "inputs larger than L2"},
+            "cpu_baseline": samp,
+            "e2e": {"value": v, "unit": "GStencil/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def timed_runs(uhs, st, a, b, params, steps, warmup, stream, dist=None):
+    import torch
+    for _ in range(warmup):
+        uhs.run(st, a, b, params, stream=stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    n0 = uhs.launch_count()
+    e0.record(stream)
+    for _ in range(steps):
+        uhs.run(st, a, b, params, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    return ms, uhs.launch_count() - n0
+
+
+def main():
+    args = parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    import uxxxxxxxxh_gb300 as uhs
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist_mod.init_process_group("nccl", device_id=torch.device("cuda", local))
+        dist = dist_mod
+
+    st, a0 = make_workload(args)
+    params = uhs.RunParams(kernel=args.kernel, arith=args.arith, flags=uhs._lib.UHS_FLAG_NO_SYNC)
+    stream = torch.cuda.Stream()
+    dev_a = torch.from_numpy(a0.reshape(st.sizes)).cuda()
+    dev_b = dev_a.clone()
+    torch.cuda.synchronize()
+
+    clocks = Clocks(local)
+    clocks.start()
+    with torch.cuda.stream(stream):
+        ms, launches = timed_runs(uhs, st, dev_a, dev_b, params, args.steps, args.warmup, stream, dist)
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    pts = st.interior_points * st.iterations
+    value = world * pts * args.steps / (ms * 1e-3) / 1e9
+    ms_step = ms / args.steps
+    plan = uhs.plan(st, dev_a, params)
+
+    # Roofline of the sweep kernel: algorithmic bytes per launch / avg launch time.
+    eb = st.elem_bytes
+    launches_per_step = max(1, launches // max(1, args.steps))
+    avg_launch_s = (ms * 1e-3) / max(1, launches)
+    alg_bytes = 2 * eb * st.interior_points
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / avg_launch_s / 1e9
+
+    # Correctness of this exact run against the oracle (fresh input).
+    errs = None
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        import oracle
+        oracle.set_threads(os.cpu_count() or 1)
+        cpu = cpu_sample(st, a0)
+        ra, rb = a0.copy(), a0.copy()
+        oracle.iterate_f64(st, ra, rb)
+        dev_a.copy_(torch.from_numpy(a0.reshape(st.sizes)))
+        dev_b.copy_(dev_a)
+        uhs.run(st, dev_a, dev_b, uhs.RunParams(kernel=args.kernel, arith=args.arith))
+        got = dev_a.cpu().numpy().reshape(-1)
+        errs = oracle.error(st, ra, got)
+        errs["halo_bit_exact"] = oracle.halo_diff(st, ra, got) == 0
+
+    # FP32 grids on the same workload.
+    fp32 = None
+    if not args.no_fp32 and st.dtype == uhs.UHS_F64:
+        st32 = st.with_(dtype=uhs.UHS_F32)
+        a32 = torch.from_numpy(a0.astype(np.float32).reshape(st.sizes)).cuda()
+        b32 = a32.clone()
+        with torch.cuda.stream(stream):
+            ms32, _ = timed_runs(uhs, st32, a32, b32, uhs.RunParams(flags=uhs._lib.UHS_FLAG_NO_SYNC),
+                                 args.steps, args.warmup, stream, dist)
+        fp32 = {"value": pts * args.steps / (ms32 * 1e-3) / 1e9, "unit": "GStencil/s",
+                "speedup_vs_f64": ms / ms32}
+        if errs is not None:
+            a32.copy_(torch.from_numpy(a0.astype(np.float32).reshape(st.sizes)))
+            b32.copy_(a32)
+            uhs.run(st32, a32, b32)
+            e = oracle.error(st, ra, a32.cpu().numpy().reshape(-1))
+            fp32["l2_rel_vs_f64_oracle"] = e["l2_rel"]
+            fp32["max_rel_vs_f64_oracle"] = e["max_rel"]
+        del a32, b32
+
+    # End to end through the C ABI with host buffers.
+    e2e = None
+    if not args.no_e2e:
+        host_in = torch.from_numpy(a0.reshape(st.sizes)).pin_memory()
+        host_out = torch.empty_like(host_in).pin_memory()
+        with torch.cuda.stream(stream):
+            for it in range(args.warmup + args.steps):
+                if it == args.warmup:
+                    torch.cuda.synchronize()
+                    if dist:
+                        dist.barrier()
+                    f0 = torch.cuda.Event(enable_timing=True)
+                    f1 = torch.cuda.Event(enable_timing=True)
+                    f0.record(stream)
+                dev_a.copy_(host_in, non_blocking=True)
+                dev_b.copy_(dev_a, non_blocking=True)
+                uhs.run(st, dev_a, dev_b, params, stream=stream)
+                host_out.copy_(dev_a, non_blocking=True)
+            f1.record(stream)
+            torch.cuda.synchronize()
+        ems = f0.elapsed_time(f1)
+        if dist:
+            t = torch.tensor([ems], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ems = float(t.item())
+        nbytes = host_in.numel() * host_in.element_size()
+        e2e = {"value": world * pts * args.steps / (ems * 1e-3) / 1e9, "unit": "GStencil/s",
+               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": ems / args.steps}
+
+    if rank != 0:
+        return
+    name = {0: "f64", 1: "f32"}.get(st.dtype, "f32x2")
+    arith_names = {1: "fma", 2: "exact", 3: "df32"}
+    line = {
+        "metric": "GStencil/s", "value": value, "unit": "GStencil/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": name, "data": "synthetic (seeded SplitMix64)",
+        "config": {"workload": f"{st.name}: {'x'.join(str(u - l) for l, u in zip(st.lb, st.ub))} interior, "
+                               f"halo {st.lb[2]}, T={st.iterations}",
+                   "parallelism": "replicas" if world > 1 else "1 GPU", "l2": "inputs larger than L2 (no flush)",
+                   "kernel": plan.kernel, "arith": arith_names.get(plan.arith, plan.arith),
+                   "tile": [plan.tile_x, plan.tile_y, plan.tile_z], "k_temporal": plan.k_temporal},
+        "pct_hbm_roofline": achieved / peak,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_launch_s * 1e3},
+        "gpu_launches": launches,
+        "launches_per_step": launches_per_step,
+        "clocks": clk,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "error_vs_oracle": errs,
+        "fp32": fp32,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

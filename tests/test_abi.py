@@ -1,0 +1,95 @@
+"""The C-ABI library loads, exports every entry point include/*.h declares,
+and rejects malformed calls with the documented status codes -- all without
+a GPU (validation never touches the device)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+import uxxxxxxxxh_gb300 as uhs
+from uxxxxxxxxh_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_functions():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if not fn.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", fn)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b(\w+)\s*\(", text, flags=re.M):
+            name = m.group(1)
+            if name not in ("if", "for", "while", "return", "sizeof") and not text[m.start():].startswith("#"):
+                names.add(name)
+    return sorted(n for n in names if n.startswith(("uhs_", "_mlir_ciface_")))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = uhs.lib()
+    declared = _declared_functions()
+    assert "uhs_run" in declared and "uhs_dsl_parse" in declared
+    for name in declared:
+        assert hasattr(lib, name), f"libuhs.so does not export {name}"
+        assert name in _lib.SIGNATURES, f"{name} has no ctypes signature in _lib.SIGNATURES"
+
+
+def test_abi_version():
+    assert uhs.lib().uhs_abi_version() == 1
+
+
+def _grid(st, ptr=0x10000):
+    return uhs.memref_raw(ptr, st.sizes)
+
+
+def _st(**kw):
+    st = uhs.make_stencil("t", 3, (8, 8, 8), 1, uhs.star_offsets(3, 1), [1 / 7] * 7, iterations=2)
+    return st.with_(**kw)
+
+
+def _validate(st, a, b):
+    d = st.to_desc()
+    return uhs.lib().uhs_validate(d.ref(), ctypes.byref(a), ctypes.byref(b))
+
+
+def test_validate_accepts_a_good_program():
+    st = _st()
+    assert _validate(st, _grid(st, 0x10000), _grid(st, 0x20000)) == _lib.UHS_OK
+
+
+@pytest.mark.parametrize("mutate,code", [
+    (dict(iterations=3), _lib.UHS_EINVAL),          # odd T > 1 (MLIRGen.cpp:317)
+    (dict(rank=4), _lib.UHS_EINVAL),
+    (dict(dtype=9), _lib.UHS_EINVAL),
+    (dict(lb=(0, 1, 1)), _lib.UHS_EINVAL),          # z-1 reaches below the grid
+    (dict(ub=(10, 9, 9)), _lib.UHS_EINVAL),         # z+1 reaches past the grid
+    (dict(terms=[(5, 0, 0, 1.0)]), _lib.UHS_EUNSUPPORTED),
+    (dict(terms=[]), _lib.UHS_EUNSUPPORTED),
+])
+def test_validate_rejects(mutate, code):
+    st = _st(**mutate)
+    assert _validate(st, _grid(st, 0x10000), _grid(st, 0x20000)) == code
+    assert uhs.lib().uhs_last_error()
+
+
+def test_validate_rejects_bad_memrefs():
+    st = _st()
+    a, b = _grid(st, 0x10000), _grid(st, 0x20000)
+    assert _validate(st, a, _grid(st, 0x10000)) == _lib.UHS_EINVAL          # same grid twice
+    b.strides[2] = 2
+    assert _validate(st, a, b) == _lib.UHS_EUNSUPPORTED                     # non-unit x stride
+    b = _grid(st, 0x20000)
+    b.sizes[1] = 9
+    assert _validate(st, a, b) == _lib.UHS_EINVAL                           # shapes differ
+    b = _grid(st, 0x20004)
+    assert _validate(st, a, b) == _lib.UHS_EINVAL                           # misaligned doubles
+    assert _validate(st, a, uhs.memref_raw(0, st.sizes)) == _lib.UHS_EINVAL  # NULL
+
+
+def test_errors_raise_in_python():
+    st = _st(iterations=5)
+    with pytest.raises(uhs.UhsError) as ei:
+        uhs.validate(st, _grid(st, 0x10000), _grid(st, 0x20000))
+    assert "multiple of 2" in str(ei.value)
