@@ -50,7 +50,8 @@ enum {
 enum {
     UHS_F64 = 0,  /* double grids (the reference's type in every case) */
     UHS_F32 = 1,  /* float grids, float arithmetic */
-    UHS_F32X2 = 2 /* compensated pair: two float grids, value = hi + lo */
+    UHS_F32X2 = 2 /* compensated pair: each 8-byte element is {float hi, float lo},
+                     value = hi + lo (about 48 significant bits) */
 };
 
 enum {
@@ -113,11 +114,14 @@ typedef struct uhs_params {
     int32_t kernel;       /* UHS_KERNEL_* */
     int32_t arith;        /* UHS_ARITH_* */
     int32_t tile_x;       /* CTA tile along x (fastest axis) */
-    int32_t tile_y;       /* CTA tile along y */
-    int32_t tile_z;       /* planes streamed per CTA along the slowest axis (0 = all) */
+    int32_t tile_y;       /* CTA tile along y (rank 3) */
+    int32_t tile_z;       /* planes streamed per CTA along the slowest axis */
     int32_t k_temporal;   /* timesteps fused per pass over HBM */
-    int32_t use_tma;      /* -1 off, 0 auto, 1 on */
+    int32_t use_tma;      /* -1 off (cp.async loads), 0 auto, 1 on */
     int32_t flags;        /* UHS_FLAG_* */
+    int32_t vy;           /* points per thread along y (streaming kernel, rank 3) */
+    int32_t prefetch;     /* planes loaded ahead of the plane being computed */
+    int32_t reserved[2];
 } uhs_params;
 
 enum {

@@ -1,0 +1,152 @@
+"""Parity of the 2.5D streaming kernels (UHS_KERNEL_STREAM) with the oracle.
+
+FP64 grids in FMA or float-pair (df32) arithmetic must stay within a max
+error of 1e-12 relative to the field's largest magnitude after T steps, the
+halo bit-exact; FP32 grids within a relative L2 error of 1e-6 of the FP64
+oracle; float-pair grids (UHS_F32X2) within 1e-12.  Both loaders (TMA tensor
+copies and cp.async) and every tile variant are exercised.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import uxxxxxxxxh_gb300 as uhs
+from gpu_util import assert_f64_close, assert_halo_exact, run_gpu, run_oracle
+from uxxxxxxxxh_gb300.workloads import random_case
+
+pytestmark = pytest.mark.gpu
+
+ODD_3D = (21, 35, 70)
+ODD_2D = (133, 301)
+STREAM = uhs.UHS_KERNEL_STREAM
+
+
+def _case(rank, r, kind, T=4, seed=7, interior=None):
+    interior = interior or (ODD_3D if rank == 3 else ODD_2D)
+    return random_case(rank, r, kind, interior, T, seed)
+
+
+@pytest.mark.parametrize("arith", [uhs.UHS_ARITH_FMA, uhs.UHS_ARITH_DF32])
+@pytest.mark.parametrize("use_tma", [1, -1])
+@pytest.mark.parametrize("rank,r,kind", uhs.SHAPES)
+def test_stream_f64(cuda, rank, r, kind, arith, use_tma):
+    # TMA needs 16-byte row pitches: an even padded row length for doubles
+    interior = None if use_tma < 0 or rank == 3 else (ODD_2D[0], ODD_2D[1] + 1)
+    st, a0 = _case(rank, r, kind, interior=interior)
+    ra, rb = run_oracle(st, a0)
+    p = uhs.RunParams(kernel=STREAM, arith=arith, use_tma=use_tma)
+    assert uhs.plan(st, params=p).kernel == STREAM
+    ga, gb = run_gpu(st, a0, p)
+    assert_f64_close(st, ra, ga)
+    assert_f64_close(st, rb, gb)
+    assert_halo_exact(st, ra, ga)
+    assert_halo_exact(st, rb, gb)
+
+
+@pytest.mark.parametrize("rank,r,kind", uhs.SHAPES)
+def test_stream_f32(cuda, rank, r, kind):
+    import torch
+    st, a0 = _case(rank, r, kind)
+    a32 = a0.astype(np.float32)
+    ra, _ = run_oracle(st, a32.astype(np.float64))
+    st32 = st.with_(dtype=uhs.UHS_F32)
+    ga, _ = run_gpu(st32, a32, uhs.RunParams(kernel=STREAM), dtype=torch.float32)
+    e = oracle.error(st, ra, ga)
+    assert e["l2_rel"] <= 1e-6, e
+    assert oracle.halo_diff(st32, a32, ga) == 0
+
+
+def _pairs(a: np.ndarray) -> np.ndarray:
+    hi = a.astype(np.float32)
+    lo = (a - hi.astype(np.float64)).astype(np.float32)
+    return np.stack([hi, lo], axis=-1).reshape(-1).view(np.float64)
+
+
+def _unpair(p: np.ndarray) -> np.ndarray:
+    f = p.view(np.float32).reshape(-1, 2).astype(np.float64)
+    return f[:, 0] + f[:, 1]
+
+
+@pytest.mark.parametrize("rank,r,kind", [(3, 1, "star"), (3, 2, "box"), (2, 3, "star"), (2, 1, "box")])
+@pytest.mark.parametrize("use_tma", [1, -1])
+def test_stream_f32x2_pairs(cuda, rank, r, kind, use_tma):
+    interior = None if use_tma < 0 or rank == 3 else (ODD_2D[0], ODD_2D[1] + 1)
+    st, a0 = _case(rank, r, kind, interior=interior)
+    pairs = _pairs(a0)
+    start = _unpair(pairs)
+    ra, _ = run_oracle(st, start)
+    stp = st.with_(dtype=uhs.UHS_F32X2)
+    ga, _ = run_gpu(stp, pairs, uhs.RunParams(kernel=STREAM, use_tma=use_tma))
+    assert_f64_close(st, ra, _unpair(ga))
+    assert oracle.halo_diff(stp, pairs, ga) == 0
+
+
+@pytest.mark.parametrize("tile_x,tile_y,vy", [(32, 32, 4), (32, 16, 4), (64, 8, 2), (32, 16, 2)])
+@pytest.mark.parametrize("arith", [uhs.UHS_ARITH_FMA, uhs.UHS_ARITH_DF32])
+def test_stream_tile_variants_3d(cuda, tile_x, tile_y, vy, arith):
+    st, a0 = _case(3, 2, "star", T=2, interior=(40, 37, 130))
+    ra, _ = run_oracle(st, a0)
+    for tma in (1, -1):
+        p = uhs.RunParams(kernel=STREAM, arith=arith, tile_x=tile_x, tile_y=tile_y, vy=vy, use_tma=tma)
+        got = uhs.plan(st, params=p)
+        assert (got.tile_x, got.tile_y, got.vy) == (tile_x, tile_y, vy)
+        ga, _ = run_gpu(st, a0, p)
+        assert_f64_close(st, ra, ga)
+
+
+@pytest.mark.parametrize("tile_x", [64, 128, 256])
+def test_stream_tile_variants_2d(cuda, tile_x):
+    st, a0 = _case(2, 1, "box", T=2, interior=(90, 1000))
+    ra, _ = run_oracle(st, a0)
+    ga, _ = run_gpu(st, a0, uhs.RunParams(kernel=STREAM, tile_x=tile_x))
+    assert_f64_close(st, ra, ga)
+
+
+def test_stream_offset_domain_exercises_tma_shift(cuda):
+    """Domain starting one cell past the halo: the TMA box start is rounded
+    down to its 16-byte granule and the kernel indexes from the remainder."""
+    st, a0 = _case(3, 1, "star", T=2, interior=(12, 20, 50))
+    st = st.with_(lb=(1, 1, 2), ub=(st.ub[0], st.ub[1], st.ub[2] - 3))
+    ra, _ = run_oracle(st, a0)
+    for arith in (uhs.UHS_ARITH_FMA, uhs.UHS_ARITH_DF32):
+        ga, _ = run_gpu(st, a0, uhs.RunParams(kernel=STREAM, arith=arith, use_tma=1))
+        assert_f64_close(st, ra, ga)
+        assert_halo_exact(st, ra, ga)
+
+
+def test_stream_z_chunks_and_small_grids(cuda):
+    for interior, tz in [((1, 1, 1), 0), ((5, 3, 33), 1), ((64, 8, 40), 7), ((30, 30, 30), 1000)]:
+        st, a0 = random_case(3, 3, "star", interior, 2, 3)
+        ra, _ = run_oracle(st, a0)
+        ga, _ = run_gpu(st, a0, uhs.RunParams(kernel=STREAM, arith=uhs.UHS_ARITH_DF32, tile_z=tz))
+        assert_f64_close(st, ra, ga)
+
+
+def test_df32_range_error_is_reported(cuda):
+    st, a0 = _case(3, 1, "star", T=2, interior=(8, 8, 40))
+    a0[len(a0) // 2] = 1e300
+    with pytest.raises(uhs.UhsError) as ei:
+        run_gpu(st, a0, uhs.RunParams(kernel=STREAM, arith=uhs.UHS_ARITH_DF32))
+    assert ei.value.code == uhs._lib.UHS_ERANGE
+    # the device status word is cleared: a following in-range run succeeds
+    st2, b0 = _case(3, 1, "star", T=2, interior=(8, 8, 40))
+    ra, _ = run_oracle(st2, b0)
+    ga, _ = run_gpu(st2, b0, uhs.RunParams(kernel=STREAM, arith=uhs.UHS_ARITH_DF32))
+    assert_f64_close(st2, ra, ga)
+
+
+def test_df32_handles_zeros_tiny_and_negative_values(cuda):
+    st, a0 = _case(3, 1, "box", T=2, interior=(10, 10, 40))
+    a0[::7] = 0.0
+    a0[1::11] = -a0[1::11]
+    a0[2::13] *= 1e-30
+    ra, _ = run_oracle(st, a0)
+    ga, _ = run_gpu(st, a0, uhs.RunParams(kernel=STREAM, arith=uhs.UHS_ARITH_DF32))
+    assert_f64_close(st, ra, ga)
+
+
+def test_forced_tma_on_unaligned_rows_is_refused(cuda):
+    st, a0 = _case(2, 1, "star", interior=(20, 301))  # 303 doubles per row
+    with pytest.raises(uhs.UhsError) as ei:
+        run_gpu(st, a0, uhs.RunParams(kernel=STREAM, use_tma=1))
+    assert ei.value.code == uhs._lib.UHS_EUNSUPPORTED

@@ -1,0 +1,76 @@
+// Host-visible description of a streaming-kernel launch (stream_kernel.cuh
+// holds the kernels, stream_launch.cuh the argument packing).  Shared by the
+// runtime, which plans launches, and the per-storage translation units.
+#pragma once
+#include <cuda.h>
+
+#include "uhs_kernels.h"
+
+namespace uhs {
+
+enum { kStar3 = 0, kBox3 = 1, kStar2 = 2, kBox2 = 3 };
+enum { kStF64 = 0, kStF32 = 1, kStF32x2 = 2 };
+enum { kArNative = 0, kArDf32 = 1 };
+enum { kLdCpAsync = 0, kLdTma = 1 };
+
+constexpr int ct_round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+// Everything one streaming launch needs (filled by the runtime).
+struct StreamCall {
+    int shape, R, st, ar, ld, tile, zchunk;
+    const double *coef;  // NT coefficients in coef_slot order
+    GridView in, out;    // views in the kernel's (z, y, x) frame
+    int64_t lb[3], ub[3];
+    const CUtensorMap *tmap;
+    int shift;
+    unsigned *err;
+    cudaStream_t stream;
+    int *occ_out;  // when set: report CTAs per SM of the variant instead of launching
+};
+
+// Tile variants: rank-3 (BX, TYT, VY) and rank-2 (BX).
+//   rank 3: 0 = 32 x 32 (VY 4), 1 = 32 x 16 (VY 4), 2 = 64 x 8 (VY 2), 3 = 32 x 16 (VY 2)
+//           (box stencils of radius 2 and 3 always use 32 x 16, VY 2)
+//   rank 2: 0 = 128, 1 = 64, 2 = 256 (cp.async only: a TMA box is <= 256 wide)
+struct TileShape {
+    int bx, tyt, vy;
+};
+inline TileShape tile_shape(bool is2d, int tile) {
+    if (is2d) return tile == 1 ? TileShape{64, 1, 1} : tile == 2 ? TileShape{256, 1, 1} : TileShape{128, 1, 1};
+    switch (tile) {
+        case 1: return TileShape{32, 4, 4};
+        case 2: return TileShape{64, 4, 2};
+        case 3: return TileShape{32, 8, 2};
+        default: return TileShape{32, 8, 4};
+    }
+}
+
+// Per translation unit entry points (stream_<storage>_<rank>.cu).
+cudaError_t launch_stream_f64n_3d(const StreamCall &c);
+cudaError_t launch_stream_f64df_3d(const StreamCall &c);
+cudaError_t launch_stream_f32_3d(const StreamCall &c);
+cudaError_t launch_stream_f32x2_3d(const StreamCall &c);
+cudaError_t launch_stream_f64n_2d(const StreamCall &c);
+cudaError_t launch_stream_f64df_2d(const StreamCall &c);
+cudaError_t launch_stream_f32_2d(const StreamCall &c);
+cudaError_t launch_stream_f32x2_2d(const StreamCall &c);
+
+// Geometry of a variant as the kernel template computes it (host mirror).
+inline void stream_box(const StreamCall &c, int eb, int *W, int *H) {
+    const bool is2d = c.shape == kStar2 || c.shape == kBox2;
+    const TileShape t = tile_shape(is2d, c.tile);
+    const int q = 16 / eb;
+    const bool big_box = (c.shape == kBox3 && c.R >= 2);
+    const int bx = big_box ? 32 : t.bx, by = big_box ? 16 : t.tyt * t.vy;
+    *W = ct_round_up(bx + 2 * c.R + (c.ld == kLdTma ? q - 1 : 0), q);
+    *H = by + (is2d ? 0 : 2 * c.R);
+}
+inline void stream_tile_xy(const StreamCall &c, int *bx, int *by) {
+    const bool is2d = c.shape == kStar2 || c.shape == kBox2;
+    const TileShape t = tile_shape(is2d, c.tile);
+    const bool big_box = (c.shape == kBox3 && c.R >= 2);
+    *bx = big_box ? 32 : t.bx;
+    *by = big_box ? 16 : t.tyt * t.vy;
+}
+
+}  // namespace uhs

@@ -1,0 +1,7 @@
+// Streaming-kernel variants for one storage/arithmetic pair and rank
+// (instantiated in their own translation unit so builds run in parallel).
+#include "stream_launch.cuh"
+
+namespace uhs {
+cudaError_t launch_stream_f64n_2d(const StreamCall &c) { return dispatch_shape<kStF64, kArNative, true>(c); }
+}  // namespace uhs

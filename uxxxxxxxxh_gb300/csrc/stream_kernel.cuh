@@ -1,0 +1,422 @@
+// 2.5D streaming sweep kernels for star and box stencils of radius 1..3.
+//
+// One CTA owns a BX x BY tile of the (y, x) plane and walks a chunk of planes
+// along the slowest axis z (for a rank-2 grid the rows play the part of the
+// planes and the tile is one row segment).  Each input plane of the tile,
+// halo included, is fetched from HBM once per CTA into a ring of shared-
+// memory slots, either by one TMA tensor copy per plane (completion on an
+// mbarrier) or by cp.async from every thread; loads run PD planes ahead of
+// the plane being computed.  For star stencils the z-neighbours of each
+// thread's points live in a register queue (the 2.5D register-streaming
+// scheme: a plane's own column is read from shared memory once and then
+// shifts through registers), so shared memory holds only the planes whose
+// in-plane neighbours are still needed; box stencils keep the 2R+1 planes a
+// point touches.  Each thread computes VY points stacked along y and reuses
+// the column it reads from shared memory across them.
+//
+// Arithmetic policies:
+//   native  double grids in DFMA, float grids in FFMA;
+//   df32    double grids split once per element into float pairs (integer
+//           bit operations, no FP64 instruction), swept with error-free
+//           float-pair products and sums, joined back to double on store;
+//           float-pair grids (UHS_F32X2, interleaved {hi, lo}) use the same
+//           arithmetic without the split and join.
+// The reference emits one generic NVVM kernel per stencil for this step
+// (examples/2d5pt_star/2d5pt_gpu.mlir:10-102): scalar loads into a shared
+// input tile, a barrier, per-thread sums into a shared output tile, a second
+// barrier and a write-back.
+#pragma once
+#include <cuda.h>
+
+#include <type_traits>
+
+#include "df32.cuh"
+#include "stream_call.h"
+
+namespace uhs {
+
+
+template <int SHAPE, int R>
+struct ShapeInfo {
+    static constexpr bool is2d = SHAPE >= 2;
+    static constexpr bool star = (SHAPE == kStar3 || SHAPE == kStar2);
+    static constexpr int RY = is2d ? 0 : R;
+    static constexpr int D = 2 * R + 1;
+    static constexpr int NT = star ? (is2d ? 4 * R + 1 : 6 * R + 1) : (is2d ? D * D : D * D * D);
+};
+
+// Coefficient slot of each offset (the host writes the descriptor's
+// coefficients in this order).
+//   star3: z(-1,+1,-2,+2..), y(..), x(..), centre      star2: z(..), x(..), centre
+//   box3 : ((dz+R)*D + dy+R)*D + dx+R                  box2 : (dz+R)*D + dx+R
+template <int SHAPE, int R>
+__host__ __device__ constexpr int coef_slot(int dz, int dy, int dx) {
+    constexpr int D = 2 * R + 1;
+    if (SHAPE == kBox3) return ((dz + R) * D + (dy + R)) * D + (dx + R);
+    if (SHAPE == kBox2) return (dz + R) * D + (dx + R);
+    const int axes = SHAPE == kStar3 ? 3 : 2;
+    if (dz == 0 && dy == 0 && dx == 0) return axes * 2 * R;
+    int axis, d;
+    if (dz != 0) {
+        axis = 0;
+        d = dz;
+    } else if (dy != 0) {
+        axis = 1;
+        d = dy;
+    } else {
+        axis = SHAPE == kStar3 ? 2 : 1;
+        d = dx;
+    }
+    const int ad = d < 0 ? -d : d;
+    return axis * 2 * R + (ad - 1) * 2 + (d > 0 ? 1 : 0);
+}
+
+template <int SHAPE_, int R_, int ST_, int AR_, int LD_, int BX_, int TYT_, int VY_, int PD_>
+struct StreamCfg {
+    static constexpr int SHAPE = SHAPE_, R = R_, ST = ST_, AR = AR_, LD = LD_, BX = BX_, TYT = TYT_, VY = VY_,
+                         PD = PD_;
+    using SI = ShapeInfo<SHAPE, R>;
+    using TS = std::conditional_t<ST == kStF64, double, std::conditional_t<ST == kStF32, float, float2>>;
+    static constexpr bool CONVERT = (ST == kStF64 && AR == kArDf32);
+    using TC = std::conditional_t<CONVERT, float2, TS>;
+    static constexpr int EB = sizeof(TS);
+    static constexpr int Q = 16 / EB;  // TMA x-coordinate granule, elements
+    static constexpr int RY = SI::RY;
+    static constexpr int BY = TYT * VY;
+    static constexpr int W = ct_round_up(BX + 2 * R + (LD == kLdTma ? Q - 1 : 0), Q);
+    static constexpr int H = BY + 2 * RY;
+    static constexpr int NCMP = SI::star ? R + 1 : 2 * R + 1;
+    static constexpr int NSTG = CONVERT ? PD + 1 : NCMP + PD;
+    static constexpr int STG_SLOT = ct_round_up(W * H * EB, 128);
+    static constexpr int CMP_SLOT = ct_round_up(W * H * (int)sizeof(TC), 128);
+    static constexpr int SMEM = NSTG * STG_SLOT + (CONVERT ? NCMP * CMP_SLOT : 0) + NSTG * 8;
+    static constexpr int THREADS = BX * TYT;
+    static constexpr int NT = SI::NT;
+    static_assert(LD != kLdTma || W <= 256, "TMA boxes are at most 256 elements wide");
+    static_assert(!SI::is2d || (TYT == 1 && VY == 1), "rank-2 tiles are one row");
+};
+
+template <int NT>
+struct StreamArgs {
+    CUtensorMap tmap;  // TMA loader only
+    const void *in;
+    void *out;
+    int64_t in_s0, in_s1, out_s0, out_s1;
+    int64_t n0, n1, n2;
+    int64_t lb0, lb1, lb2, ub0, ub1, ub2;
+    int zchunk;
+    int shift;  // TMA box starts this many elements left of x0 - R (16-byte granule)
+    unsigned *err;
+    double cd[NT];
+    float ch[NT], cl[NT];
+};
+
+// ---- asynchronous copy primitives --------------------------------------
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem, bool valid) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    const int n = valid ? BYTES : 0;
+    if constexpr (BYTES == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(n) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(bar));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(a), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+    const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(bar));
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(a), "r"(bytes) : "memory");
+}
+// Bounded wait for phase `parity` of an mbarrier: false when the bound ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
+    const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(bar));
+    for (int i = 0; i < (1 << 22); ++i) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void tma_load_3d(void *smem, const CUtensorMap *map, int x, int y, int z, uint64_t *bar) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    const unsigned b = static_cast<unsigned>(__cvta_generic_to_shared(bar));
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(s),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(b)
+        : "memory");
+}
+
+// ---- arithmetic policies -----------------------------------------------
+template <class C, int AR = C::AR>
+struct Arith;
+
+template <class C>
+struct Arith<C, kArNative> {
+    using TS = typename C::TS;
+    using Acc = TS;
+    __device__ static __forceinline__ TS coef(const StreamArgs<C::NT> &a, int k) {
+        if constexpr (std::is_same_v<TS, double>) return a.cd[k];
+        else return a.ch[k];
+    }
+    __device__ static __forceinline__ void first(Acc &acc, const StreamArgs<C::NT> &a, int k, TS v) {
+        acc = coef(a, k) * v;
+    }
+    __device__ static __forceinline__ void add(Acc &acc, const StreamArgs<C::NT> &a, int k, TS v) {
+        acc = fma(coef(a, k), v, acc);
+    }
+    __device__ static __forceinline__ void store(TS *p, const Acc &acc) { *p = acc; }
+};
+
+template <class C>
+struct Arith<C, kArDf32> {
+    using Acc = df;
+    __device__ static __forceinline__ void first(Acc &acc, const StreamArgs<C::NT> &a, int k, float2 v) {
+        df_mul(acc, a.ch[k], a.cl[k], v);
+    }
+    __device__ static __forceinline__ void add(Acc &acc, const StreamArgs<C::NT> &a, int k, float2 v) {
+        df_fma(acc, a.ch[k], a.cl[k], v);
+    }
+    __device__ static __forceinline__ void store(typename C::TS *p, const Acc &acc) {
+        if constexpr (C::ST == kStF64) *p = join_f64(acc.h, acc.l);
+        else *p = renorm(acc);
+    }
+};
+
+// ---- the kernel ---------------------------------------------------------
+template <class C>
+__global__ void __launch_bounds__(C::THREADS) k_stream(const __grid_constant__ StreamArgs<C::NT> a) {
+    using TS = typename C::TS;
+    using TC = typename C::TC;
+    using A = Arith<C>;
+    using Acc = typename A::Acc;
+    constexpr int R = C::R, RY = C::RY, BX = C::BX, TYT = C::TYT, VY = C::VY, W = C::W, H = C::H;
+    constexpr int NSTG = C::NSTG, NCMP = C::NCMP, PD = C::PD;
+    constexpr int STG_ELEMS = C::STG_SLOT / C::EB, CMP_ELEMS = C::CMP_SLOT / (int)sizeof(TC);
+    constexpr bool STAR = C::SI::star, IS2D = C::SI::is2d;
+    constexpr int NLOAD_ROWS = (H + TYT - 1) / TYT;  // cp.async: rows per thread
+    extern __shared__ __align__(128) unsigned char smem[];
+
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
+    const int64_t x0 = a.lb2 + static_cast<int64_t>(blockIdx.x) * BX;
+    const int64_t y0 = a.lb1 + static_cast<int64_t>(blockIdx.y) * C::BY;
+    const int64_t zs = a.lb0 + static_cast<int64_t>(blockIdx.z) * a.zchunk;
+    const int64_t ze = min(zs + static_cast<int64_t>(a.zchunk), a.ub0);
+    const int64_t gx0 = x0 - R - a.shift, gy0 = y0 - RY;
+    const int64_t qbeg = zs - R;
+    const int nq = static_cast<int>(ze + R - qbeg);
+    TS *const stg_base = reinterpret_cast<TS *>(smem);
+    TC *const cmp_base = C::CONVERT ? reinterpret_cast<TC *>(smem + NSTG * C::STG_SLOT) : reinterpret_cast<TC *>(smem);
+    uint64_t *const mbar = reinterpret_cast<uint64_t *>(smem + NSTG * C::STG_SLOT + (C::CONVERT ? NCMP * C::CMP_SLOT : 0));
+    constexpr int CMP_STRIDE = C::CONVERT ? CMP_ELEMS : STG_ELEMS;
+    constexpr int NRING = C::CONVERT ? NCMP : NSTG;  // ring the compute reads
+
+    if constexpr (C::LD == kLdTma) {
+        if (tid == 0) {
+            for (int s = 0; s < NSTG; ++s) mbar_init(mbar + s, 1);
+            asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        }
+        __syncthreads();
+    }
+
+    // cp.async: per-thread row offsets inside a plane (32-bit: a plane holds
+    // fewer than 2^31 elements, which the host checks) and validity.
+    int row_off[NLOAD_ROWS];
+    bool row_ok[NLOAD_ROWS];
+#pragma unroll
+    for (int i = 0; i < NLOAD_ROWS; ++i) {
+        const int r = ty + i * TYT;
+        const int64_t gy = gy0 + r;
+        row_ok[i] = r < H && gy >= 0 && gy < a.n1;
+        row_off[i] = row_ok[i] ? static_cast<int>(gy * a.in_s1) : 0;
+    }
+    const int gxa = static_cast<int>(gx0) + tx, gxb = gxa + BX;
+    const bool col_a = gxa >= 0 && gxa < a.n2;
+    const bool col_b = tx < 2 * R && gxb < a.n2;
+
+    auto issue = [&](int j, int slot) {
+        const int64_t p = qbeg + j;
+        if constexpr (C::LD == kLdCpAsync) {
+            const TS *plane = static_cast<const TS *>(a.in) + p * a.in_s0;
+            TS *dst = stg_base + slot * STG_ELEMS;
+#pragma unroll
+            for (int i = 0; i < NLOAD_ROWS; ++i) {
+                const int r = ty + i * TYT;
+                if (r < H) {
+                    const TS *src = plane + row_off[i];
+                    cp_async<C::EB>(dst + r * W + tx, row_ok[i] && col_a ? src + gxa : plane, row_ok[i] && col_a);
+                    if (tx < 2 * R) cp_async<C::EB>(dst + r * W + tx + BX, row_ok[i] && col_b ? src + gxb : plane,
+                                                    row_ok[i] && col_b);
+                }
+            }
+        } else {
+            if (tid == 0) {
+                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                mbar_expect_tx(mbar + slot, static_cast<unsigned>(W * H * C::EB));
+                tma_load_3d(stg_base + slot * STG_ELEMS, &a.tmap, static_cast<int>(gx0), static_cast<int>(gy0),
+                            static_cast<int>(p), mbar + slot);
+            }
+        }
+    };
+
+#pragma unroll 1
+    for (int j = 0; j < PD; ++j) {
+        if (j < nq) issue(j, j % NSTG);
+        if constexpr (C::LD == kLdCpAsync) cp_commit();
+    }
+
+    const int cx = tx + R + a.shift;  // smem column of this thread's x
+    const int own = (ty * VY + RY) * W + cx;
+    TC q[VY][STAR ? 2 * R + 1 : 1];  // star: z-queue, q[v][R + dz]
+    unsigned range_err = 0;
+    const bool x_ok = x0 + tx < a.ub2;
+    // output pointer of (zs, y0 + ty*VY, x0 + tx); rows beyond ub1 are masked
+    TS *optr = static_cast<TS *>(a.out) + zs * a.out_s0 + (y0 + ty * VY) * a.out_s1 + x0 + tx;
+    int vmax = static_cast<int>(min(static_cast<int64_t>(VY), a.ub1 - (y0 + ty * VY)));
+    if (!x_ok) vmax = 0;
+
+    int s_stg = 0;       // staging slot of plane j
+    unsigned phase = 0;  // mbarrier phase of plane j's slot
+    int s_iss = PD % NSTG;
+    int s_cmp = 0;  // compute-ring slot of plane j
+#pragma unroll 1
+    for (int j = 0; j < nq; ++j) {
+        bool ok = true;
+        if constexpr (C::LD == kLdCpAsync) {
+            cp_wait<PD - 1>();
+            __syncthreads();
+        } else {
+            ok = mbar_wait(mbar + s_stg, phase);
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) {
+                    atomicOr(a.err, kDevErrTimeout);
+                    for (int k = j; k < min(j + PD, nq); ++k)
+                        (void)mbar_wait(mbar + (k % NSTG), static_cast<unsigned>((k / NSTG) & 1));
+                }
+                return;
+            }
+        }
+        if (j + PD < nq) issue(j + PD, s_iss);
+        if constexpr (C::LD == kLdCpAsync) cp_commit();
+
+        if constexpr (C::CONVERT) {
+            // Columns the loader wrote: the whole TMA box, or BX + 2R for cp.async.
+            constexpr int WL = C::LD == kLdTma ? W : BX + 2 * R;
+            const double *sp = reinterpret_cast<const double *>(stg_base + s_stg * STG_ELEMS);
+            float2 *dp = cmp_base + s_cmp * CMP_ELEMS;
+#pragma unroll
+            for (int i = 0; i < NLOAD_ROWS; ++i) {
+                const int r = ty + i * TYT;
+                if (r < H) {
+#pragma unroll
+                    for (int c0 = 0; c0 < WL; c0 += BX)
+                        if (c0 + tx < WL) dp[r * W + c0 + tx] = split_f64(sp[r * W + c0 + tx], range_err);
+                }
+            }
+            __syncthreads();
+        }
+        const int slot_j = C::CONVERT ? s_cmp : s_stg;
+        const TC *cur = cmp_base + slot_j * CMP_STRIDE;
+        if constexpr (STAR) {
+#pragma unroll
+            for (int v = 0; v < VY; ++v) {
+#pragma unroll
+                for (int k = 0; k < 2 * R; ++k) q[v][k] = q[v][k + 1];
+                q[v][2 * R] = cur[own + v * W];
+            }
+        }
+        if (j >= 2 * R) {
+            Acc acc[VY];
+            if constexpr (STAR) {
+                const int sl = slot_j >= R ? slot_j - R : slot_j - R + NRING;
+                const TC *pl = cmp_base + sl * CMP_STRIDE;
+#pragma unroll
+                for (int v = 0; v < VY; ++v) A::first(acc[v], a, coef_slot<C::SHAPE, R>(0, 0, 0), q[v][R]);
+#pragma unroll
+                for (int d = 1; d <= R; ++d)
+#pragma unroll
+                    for (int v = 0; v < VY; ++v) {
+                        A::add(acc[v], a, coef_slot<C::SHAPE, R>(-d, 0, 0), q[v][R - d]);
+                        A::add(acc[v], a, coef_slot<C::SHAPE, R>(d, 0, 0), q[v][R + d]);
+                    }
+                if constexpr (!IS2D) {
+                    TC col[VY + 2 * R];
+#pragma unroll
+                    for (int i = 0; i < VY + 2 * R; ++i) col[i] = pl[own + (i - R) * W];
+#pragma unroll
+                    for (int d = 1; d <= R; ++d)
+#pragma unroll
+                        for (int v = 0; v < VY; ++v) {
+                            A::add(acc[v], a, coef_slot<C::SHAPE, R>(0, -d, 0), col[v + R - d]);
+                            A::add(acc[v], a, coef_slot<C::SHAPE, R>(0, d, 0), col[v + R + d]);
+                        }
+                }
+#pragma unroll
+                for (int d = 1; d <= R; ++d)
+#pragma unroll
+                    for (int v = 0; v < VY; ++v) {
+                        const TC *row = pl + own + v * W;
+                        A::add(acc[v], a, coef_slot<C::SHAPE, R>(0, 0, -d), row[-d]);
+                        A::add(acc[v], a, coef_slot<C::SHAPE, R>(0, 0, d), row[d]);
+                    }
+            } else {
+#pragma unroll
+                for (int dz = -R; dz <= R; ++dz) {
+                    const int back = R - dz;  // plane j - R + dz is `back` planes behind j
+                    const int sl = slot_j >= back ? slot_j - back : slot_j - back + NRING;
+                    const TC *pl = cmp_base + sl * CMP_STRIDE;
+                    if constexpr (IS2D) {
+#pragma unroll
+                        for (int dx = -R; dx <= R; ++dx) {
+                            const TC v0 = pl[own + dx];
+                            if (dz == -R && dx == -R) A::first(acc[0], a, coef_slot<C::SHAPE, R>(dz, 0, dx), v0);
+                            else A::add(acc[0], a, coef_slot<C::SHAPE, R>(dz, 0, dx), v0);
+                        }
+                    } else {
+#pragma unroll
+                        for (int dx = -R; dx <= R; ++dx) {
+                            TC col[VY + 2 * R];
+#pragma unroll
+                            for (int i = 0; i < VY + 2 * R; ++i) col[i] = pl[own + (i - R) * W + dx];
+#pragma unroll
+                            for (int dy = -R; dy <= R; ++dy)
+#pragma unroll
+                                for (int v = 0; v < VY; ++v) {
+                                    if (dz == -R && dx == -R && dy == -R)
+                                        A::first(acc[v], a, coef_slot<C::SHAPE, R>(dz, dy, dx), col[v + R + dy]);
+                                    else
+                                        A::add(acc[v], a, coef_slot<C::SHAPE, R>(dz, dy, dx), col[v + R + dy]);
+                                }
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int v = 0; v < VY; ++v)
+                if (v < vmax) A::store(optr + v * a.out_s1, acc[v]);
+            optr += a.out_s0;
+        }
+        // advance the rings
+        s_stg = s_stg + 1 == NSTG ? 0 : s_stg + 1;
+        if (s_stg == 0) phase ^= 1u;
+        s_iss = s_iss + 1 == NSTG ? 0 : s_iss + 1;
+        if constexpr (C::CONVERT) s_cmp = s_cmp + 1 == NCMP ? 0 : s_cmp + 1;
+    }
+    if constexpr (C::CONVERT) {
+        if (range_err) atomicOr(a.err, kDevErrRange);
+    }
+}
+
+}  // namespace uhs

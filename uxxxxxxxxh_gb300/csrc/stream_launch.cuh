@@ -1,0 +1,105 @@
+// Launch side of the streaming kernels: argument packing and the table of
+// compiled variants.  Included by the per-storage translation units
+// (stream_*.cu), which instantiate the variants in parallel builds.
+#pragma once
+#include <cstring>
+
+#include "stream_call.h"
+#include "stream_kernel.cuh"
+
+namespace uhs {
+
+template <class C>
+cudaError_t launch_cfg(const StreamCall &c) {
+    StreamArgs<C::NT> a;
+    std::memset(&a, 0, sizeof a);
+    if (c.tmap) a.tmap = *c.tmap;
+    a.in = c.in.data;
+    a.out = c.out.data;
+    a.in_s0 = c.in.s[0];
+    a.in_s1 = c.in.s[1];
+    a.out_s0 = c.out.s[0];
+    a.out_s1 = c.out.s[1];
+    a.n0 = c.in.n[0];
+    a.n1 = c.in.n[1];
+    a.n2 = c.in.n[2];
+    a.lb0 = c.lb[0];
+    a.lb1 = c.lb[1];
+    a.lb2 = c.lb[2];
+    a.ub0 = c.ub[0];
+    a.ub1 = c.ub[1];
+    a.ub2 = c.ub[2];
+    a.zchunk = c.zchunk;
+    a.shift = c.shift;
+    a.err = c.err;
+    for (int k = 0; k < C::NT; ++k) {
+        const double v = c.coef[k];
+        const float h = static_cast<float>(v);
+        a.cd[k] = v;
+        a.ch[k] = h;
+        a.cl[k] = static_cast<float>(v - static_cast<double>(h));
+    }
+    const int64_t nz = c.ub[0] - c.lb[0], ny = c.ub[1] - c.lb[1], nx = c.ub[2] - c.lb[2];
+    if (!c.occ_out && (nz <= 0 || ny <= 0 || nx <= 0)) return cudaSuccess;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_stream<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    if (c.occ_out) {
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(c.occ_out, k_stream<C>, C::THREADS, C::SMEM);
+    }
+    dim3 grid(static_cast<unsigned>((nx + C::BX - 1) / C::BX), static_cast<unsigned>((ny + C::BY - 1) / C::BY),
+              static_cast<unsigned>((nz + c.zchunk - 1) / c.zchunk));
+    k_stream<C><<<grid, dim3(C::BX, C::TYT), C::SMEM, c.stream>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <int SHAPE, int R, int ST, int AR, int LD>
+cudaError_t dispatch_tile(const StreamCall &c) {
+    constexpr bool is2d = ShapeInfo<SHAPE, R>::is2d;
+    if constexpr (is2d) {
+        constexpr int PD = 4;
+        switch (c.tile) {
+            case 1: return launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 64, 1, 1, PD>>(c);
+            case 2:
+                if constexpr (LD == kLdCpAsync) return launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 256, 1, 1, PD>>(c);
+                else return cudaErrorInvalidValue;
+            default: return launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 128, 1, 1, PD>>(c);
+        }
+    } else {
+        constexpr int PD = 3;
+        constexpr bool big_box = (SHAPE == kBox3 && R >= 2);
+        if constexpr (big_box) {
+            return launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 32, 8, 2, 2>>(c);
+        } else {
+            switch (c.tile) {
+                case 1: return launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 32, 4, 4, PD>>(c);
+                case 2: return launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 64, 4, 2, PD>>(c);
+                case 3: return launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 32, 8, 2, PD>>(c);
+                default: return launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 32, 8, 4, PD>>(c);
+            }
+        }
+    }
+}
+
+template <int SHAPE, int R, int ST, int AR>
+cudaError_t dispatch_loader(const StreamCall &c) {
+    return c.ld == kLdTma ? dispatch_tile<SHAPE, R, ST, AR, kLdTma>(c) : dispatch_tile<SHAPE, R, ST, AR, kLdCpAsync>(c);
+}
+
+template <int ST, int AR, bool IS2D>
+cudaError_t dispatch_shape(const StreamCall &c) {
+    constexpr int STAR = IS2D ? kStar2 : kStar3, BOX = IS2D ? kBox2 : kBox3;
+    const bool star = (c.shape == kStar2 || c.shape == kStar3);
+    switch (c.R) {
+        case 1: return star ? dispatch_loader<STAR, 1, ST, AR>(c) : dispatch_loader<BOX, 1, ST, AR>(c);
+        case 2: return star ? dispatch_loader<STAR, 2, ST, AR>(c) : dispatch_loader<BOX, 2, ST, AR>(c);
+        case 3: return star ? dispatch_loader<STAR, 3, ST, AR>(c) : dispatch_loader<BOX, 3, ST, AR>(c);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace uhs

@@ -12,15 +12,19 @@
 //    as it stands (ConvertStencilToStandard.cpp:91-149, 339-381).
 //  * The entry is synchronous for the caller (the MLIR CUDA runtime wrappers
 //    synchronise after each launch); UHS_FLAG_NO_SYNC lifts that.
+#include "stream_call.h"
 #include "uhs_kernels.h"
 
 #include <algorithm>
+#include <map>
+#include <tuple>
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 namespace uhs {
 
@@ -58,7 +62,7 @@ unsigned *device_error_word(int device) {
     return words[device];
 }
 
-static size_t elem_bytes(int dtype) { return dtype == UHS_F64 ? 8 : 4; }
+static size_t elem_bytes(int dtype) { return dtype == UHS_F32 ? 4 : 8; }
 
 // Validate one memref against the descriptor; fill the view.
 static int view_of(const uhs_stencil_desc *d, const uhs_memref *m, const char *name, GridView *v) {
@@ -165,41 +169,319 @@ static void make_spec(const uhs_stencil_desc *d, SweepSpec *sp) {
     sp->shape = kShapeGeneric;
 }
 
-static int plan_cfg(const SweepSpec &sp, const uhs_params *p, LaunchCfg *cfg) {
+// ---------------------------------------------------------------------------
+// Planning: which kernel family, arithmetic, loader and tile run a sweep.
+// ---------------------------------------------------------------------------
+struct Plan {
+    int kernel;  // UHS_KERNEL_GENERIC / UHS_KERNEL_STREAM
+    LaunchCfg cfg;
+    // streaming kernel
+    int shape = -1, R = 0, st = 0, ar = 0, ld = kLdCpAsync, tile = 0, zchunk = 0;
+    std::vector<double> coef;  // coef_slot order
+};
+
+static int device_sms() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+    }
+    return sms;
+}
+
+static int coef_slot_rt(int shape, int R, int dz, int dy, int dx) {
+    const int D = 2 * R + 1;
+    if (shape == kBox3) return ((dz + R) * D + (dy + R)) * D + (dx + R);
+    if (shape == kBox2) return (dz + R) * D + (dx + R);
+    const int axes = shape == kStar3 ? 3 : 2;
+    if (dz == 0 && dy == 0 && dx == 0) return axes * 2 * R;
+    int axis, d;
+    if (dz != 0) {
+        axis = 0;
+        d = dz;
+    } else if (dy != 0) {
+        axis = 1;
+        d = dy;
+    } else {
+        axis = shape == kStar3 ? 2 : 1;
+        d = dx;
+    }
+    return axis * 2 * R + (std::abs(d) - 1) * 2 + (d > 0 ? 1 : 0);
+}
+
+static int nterms_of(int shape, int R) {
+    const int D = 2 * R + 1;
+    switch (shape) {
+        case kStar3: return 6 * R + 1;
+        case kStar2: return 4 * R + 1;
+        case kBox3: return D * D * D;
+        default: return D * D;
+    }
+}
+
+// Star if every offset lies on an axis, box otherwise; radius 1..3.  Rank-2
+// programs are streamed along y, so (dy, dx) become the kernel's (dz, dx).
+static bool classify(const SweepSpec &sp, int *shape, int *R) {
+    int r = 0;
+    bool on_axes = true;
+    for (int k = 0; k < sp.nterms; ++k) {
+        const int a[3] = {std::abs(sp.dz[k]), std::abs(sp.dy[k]), std::abs(sp.dx[k])};
+        r = std::max({r, a[0], a[1], a[2]});
+        if ((a[0] != 0) + (a[1] != 0) + (a[2] != 0) > 1) on_axes = false;
+    }
+    if (r < 1 || r > 3) return false;
+    *R = r;
+    if (sp.rank == 3) *shape = on_axes ? kStar3 : kBox3;
+    else *shape = on_axes ? kStar2 : kBox2;
+    return true;
+}
+
+static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &view, Plan *pl) {
     uhs_params dflt;
     uhs_params_default(&dflt);
     if (!p) p = &dflt;
-    cfg->kernel = p->kernel == UHS_KERNEL_AUTO ? UHS_KERNEL_GENERIC : p->kernel;
-    cfg->arith = p->arith == UHS_ARITH_AUTO ? UHS_ARITH_FMA : p->arith;
-    cfg->tile_x = p->tile_x;
-    cfg->tile_y = p->tile_y;
-    cfg->tile_z = p->tile_z;
-    cfg->k_temporal = p->k_temporal > 0 ? p->k_temporal : 1;
-    cfg->use_tma = p->use_tma;
-    if (cfg->kernel != UHS_KERNEL_GENERIC)
-        return set_error(UHS_EUNSUPPORTED, "kernel family %d is not available for this stencil", cfg->kernel);
-    if (cfg->arith != UHS_ARITH_FMA && cfg->arith != UHS_ARITH_EXACT)
-        return set_error(UHS_EUNSUPPORTED, "arithmetic mode %d is not available for the generic kernel", cfg->arith);
-    if (sp.dtype == UHS_F32X2)
-        return set_error(UHS_EUNSUPPORTED, "float-pair grids need the streaming kernel");
-    const int tx = cfg->tile_x > 0 ? cfg->tile_x : 32, ty = cfg->tile_y > 0 ? cfg->tile_y : 8;
-    if (tx * ty > 256) return set_error(UHS_EINVAL, "tile %d x %d exceeds 256 threads", tx, ty);
-    if (tx % 32 != 0) return set_error(UHS_EINVAL, "tile_x must be a multiple of 32 (got %d)", tx);
+    LaunchCfg &cfg = pl->cfg;
+    cfg.arith = p->arith;
+    cfg.tile_x = p->tile_x;
+    cfg.tile_y = p->tile_y;
+    cfg.tile_z = p->tile_z;
+    cfg.k_temporal = p->k_temporal > 0 ? p->k_temporal : 1;
+    cfg.use_tma = p->use_tma;
+    if (p->arith < UHS_ARITH_AUTO || p->arith > UHS_ARITH_DF32)
+        return set_error(UHS_EINVAL, "unknown arithmetic mode %d", p->arith);
+    if (p->kernel < UHS_KERNEL_AUTO || p->kernel > UHS_KERNEL_MMA)
+        return set_error(UHS_EINVAL, "unknown kernel family %d", p->kernel);
+    if (cfg.k_temporal != 1) return set_error(UHS_EUNSUPPORTED, "temporal fusion depth %d is not available", cfg.k_temporal);
+
+    int shape = -1, R = 0;
+    const bool shaped = classify(sp, &shape, &R);
+    int arith = p->arith;
+    if (arith == UHS_ARITH_AUTO) arith = sp.dtype == UHS_F32X2 ? UHS_ARITH_DF32 : UHS_ARITH_FMA;
+    if (sp.dtype == UHS_F32 && arith == UHS_ARITH_DF32)
+        return set_error(UHS_EUNSUPPORTED, "float-pair arithmetic needs F64 or F32X2 grids");
+    if (sp.dtype == UHS_F32X2 && arith != UHS_ARITH_DF32)
+        return set_error(UHS_EUNSUPPORTED, "F32X2 grids are swept in float-pair arithmetic only");
+    cfg.arith = arith;
+
+    int kernel = p->kernel;
+    const bool stream_ok = shaped && arith != UHS_ARITH_EXACT;
+    if (kernel == UHS_KERNEL_AUTO) kernel = stream_ok ? UHS_KERNEL_STREAM : UHS_KERNEL_GENERIC;
+    if (kernel == UHS_KERNEL_MMA) return set_error(UHS_EUNSUPPORTED, "the tensor-core box path is not available");
+    if (kernel == UHS_KERNEL_STREAM && !stream_ok)
+        return set_error(UHS_EUNSUPPORTED, "the streaming kernel covers star and box stencils of radius 1-3 in "
+                                           "FMA or float-pair arithmetic");
+    if (kernel == UHS_KERNEL_GENERIC) {
+        if (arith != UHS_ARITH_FMA && arith != UHS_ARITH_EXACT)
+            return set_error(UHS_EUNSUPPORTED, "the generic kernel runs FMA or EXACT arithmetic");
+        const int tx = cfg.tile_x > 0 ? cfg.tile_x : 32, ty = cfg.tile_y > 0 ? cfg.tile_y : 8;
+        if (tx * ty > 256) return set_error(UHS_EINVAL, "tile %d x %d exceeds 256 threads", tx, ty);
+        if (tx % 32 != 0) return set_error(UHS_EINVAL, "tile_x must be a multiple of 32 (got %d)", tx);
+        pl->kernel = kernel;
+        cfg.kernel = kernel;
+        return UHS_OK;
+    }
+    pl->kernel = cfg.kernel = UHS_KERNEL_STREAM;
+    pl->shape = shape;
+    pl->R = R;
+    pl->st = sp.dtype == UHS_F64 ? kStF64 : sp.dtype == UHS_F32 ? kStF32 : kStF32x2;
+    pl->ar = arith == UHS_ARITH_DF32 ? kArDf32 : kArNative;
+    const bool is2d = sp.rank == 2;
+    // tile variant from (tile_x, tile_y, vy)
+    int tile = 0;
+    if (is2d) {
+        if (cfg.tile_x == 64) tile = 1;
+        else if (cfg.tile_x == 256) tile = 2;
+        else if (cfg.tile_x != 0 && cfg.tile_x != 128)
+            return set_error(UHS_EINVAL, "rank-2 streaming tiles are 64, 128 or 256 wide (got %d)", cfg.tile_x);
+    } else {
+        if (cfg.tile_x == 64) tile = 2;
+        else if (cfg.tile_x != 0 && cfg.tile_x != 32)
+            return set_error(UHS_EINVAL, "rank-3 streaming tiles are 32 or 64 wide (got %d)", cfg.tile_x);
+        else if (cfg.tile_y == 16) tile = p->vy == 2 ? 3 : 1;
+        else if (p->vy == 2) tile = 3;
+    }
+    pl->tile = tile;
+    // the kernel keeps in-plane offsets in 32 bits
+    const int64_t plane_elems = is2d ? view.s[1] : view.s[0];
+    if (plane_elems >= (int64_t(1) << 31) || view.n[2] >= (int64_t(1) << 31)) {
+        if (p->kernel == UHS_KERNEL_STREAM)
+            return set_error(UHS_EUNSUPPORTED, "planes of 2^31 elements or more need the generic kernel");
+        pl->kernel = cfg.kernel = UHS_KERNEL_GENERIC;
+        if (arith != UHS_ARITH_FMA && arith != UHS_ARITH_EXACT)
+            return set_error(UHS_EUNSUPPORTED, "planes of 2^31 elements or more run FMA or EXACT arithmetic only");
+        return UHS_OK;
+    }
+    // loader
+    const int eb = sp.dtype == UHS_F32 ? 4 : 8;
+    bool tma_ok = cfg.use_tma >= 0 && !(is2d && tile == 2);
+    const int64_t row_b = (is2d ? view.s[1] : view.s[1]) * eb, plane_b = (is2d ? view.s[1] : view.s[0]) * eb;
+    if (reinterpret_cast<uintptr_t>(view.data) % 16 || row_b % 16 || plane_b % 16) tma_ok = false;
+    if (cfg.use_tma > 0 && !tma_ok)
+        return set_error(UHS_EUNSUPPORTED, "TMA needs 16-byte aligned grids and row/plane strides");
+    pl->ld = tma_ok ? kLdTma : kLdCpAsync;
+    // coefficients in slot order
+    pl->coef.assign(nterms_of(shape, R), 0.0);
+    for (int k = 0; k < sp.nterms; ++k) {
+        const int dz = is2d ? sp.dy[k] : sp.dz[k], dy = is2d ? 0 : sp.dy[k];
+        pl->coef[coef_slot_rt(shape, R, dz, dy, sp.dx[k])] += sp.coef[k];
+    }
     return UHS_OK;
 }
 
-static int launch_sweep(const SweepSpec &sp, const LaunchCfg &cfg, const GridView &in, const GridView &out,
+// ---- TMA tensor maps (encoded through the driver entry point) -------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(ptr);
+    });
+    return fn;
+}
+
+// Map of the kernel-frame view (z, y, x) with box {W, H, 1}.
+static bool make_tmap(const GridView &v, int eb, int W, int H, CUtensorMap *m) {
+    static std::mutex mu;
+    static std::map<std::tuple<uintptr_t, int64_t, int64_t, int64_t, int64_t, int64_t, int, int, int>, CUtensorMap>
+        cache;
+    const auto key = std::make_tuple(reinterpret_cast<uintptr_t>(v.data), v.n[0], v.n[1], v.n[2], v.s[0], v.s[1],
+                                     eb, W, H);
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+        *m = it->second;
+        return true;
+    }
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dims[3] = {static_cast<cuuint64_t>(v.n[2]), static_cast<cuuint64_t>(v.n[1]),
+                                static_cast<cuuint64_t>(v.n[0])};
+    const cuuint64_t strides[2] = {static_cast<cuuint64_t>(v.s[1] * eb), static_cast<cuuint64_t>(v.s[0] * eb)};
+    const cuuint32_t box[3] = {static_cast<cuuint32_t>(W), static_cast<cuuint32_t>(H), 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = fn(m, eb == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, v.data, dims,
+                    strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return false;
+    if (cache.size() > 256) cache.clear();
+    cache[key] = *m;
+    return true;
+}
+
+static cudaError_t stream_dispatch(const StreamCall &c) {
+    const bool is2d = c.shape == kStar2 || c.shape == kBox2;
+    if (c.st == kStF64 && c.ar == kArNative) return is2d ? launch_stream_f64n_2d(c) : launch_stream_f64n_3d(c);
+    if (c.st == kStF64) return is2d ? launch_stream_f64df_2d(c) : launch_stream_f64df_3d(c);
+    if (c.st == kStF32) return is2d ? launch_stream_f32_2d(c) : launch_stream_f32_3d(c);
+    return is2d ? launch_stream_f32x2_2d(c) : launch_stream_f32x2_3d(c);
+}
+
+// Kernel-frame view: rank-2 grids (1, Y, X) stream along Y -> (Y, 1, X).
+static GridView kernel_view(const SweepSpec &sp, const GridView &v) {
+    if (sp.rank == 3) return v;
+    GridView k = v;
+    k.n[0] = v.n[1];
+    k.n[1] = 1;
+    k.s[0] = v.s[1];
+    k.s[1] = v.s[1];
+    return k;
+}
+
+static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in, const GridView &out,
                         cudaStream_t st) {
-    cudaError_t e = launch_generic(sp, cfg, in, out, st);
-    if (e != cudaSuccess) return cuda_error(e, "sweep launch");
+    if (pl.kernel == UHS_KERNEL_GENERIC) {
+        cudaError_t e = launch_generic(sp, pl.cfg, in, out, st);
+        if (e != cudaSuccess) return cuda_error(e, "generic sweep launch");
+        return UHS_OK;
+    }
+    StreamCall c{};
+    c.shape = pl.shape;
+    c.R = pl.R;
+    c.st = pl.st;
+    c.ar = pl.ar;
+    c.ld = pl.ld;
+    c.tile = pl.tile;
+    c.coef = pl.coef.data();
+    c.in = kernel_view(sp, in);
+    c.out = kernel_view(sp, out);
+    const bool is2d = sp.rank == 2;
+    c.lb[0] = is2d ? sp.lb[1] : sp.lb[0];
+    c.ub[0] = is2d ? sp.ub[1] : sp.ub[0];
+    c.lb[1] = is2d ? 0 : sp.lb[1];
+    c.ub[1] = is2d ? 1 : sp.ub[1];
+    c.lb[2] = sp.lb[2];
+    c.ub[2] = sp.ub[2];
+    c.stream = st;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    c.err = device_error_word(dev);
+    if (!c.err) return set_error(UHS_ENOMEM, "device error word allocation failed");
+    const int eb = sp.dtype == UHS_F32 ? 4 : 8;
+    CUtensorMap tmap;
+    if (c.ld == kLdTma) {
+        int W, H;
+        stream_box(c, eb, &W, &H);
+        if (make_tmap(c.in, eb, W, H, &tmap)) {
+            c.tmap = &tmap;
+            const int q = 16 / eb;
+            c.shift = static_cast<int>(((c.lb[2] - c.R) % q + q) % q);
+        } else {
+            c.ld = kLdCpAsync;
+        }
+    }
+    // z-chunk: enough CTAs for about four waves over the SMs
+    int bx, by;
+    stream_tile_xy(c, &bx, &by);
+    const int64_t nz = c.ub[0] - c.lb[0];
+    const int64_t tiles = ((c.ub[2] - c.lb[2] + bx - 1) / bx) * ((c.ub[1] - c.lb[1] + by - 1) / by);
+    int zchunk = pl.cfg.tile_z;
+    if (zchunk <= 0 && nz > 0 && tiles > 0) {
+        int occ = 0;
+        StreamCall q = c;
+        q.occ_out = &occ;
+        if (stream_dispatch(q) != cudaSuccess || occ <= 0) occ = 1;
+        const int64_t want = static_cast<int64_t>(device_sms()) * occ * 4;
+        const int64_t chunks = std::max<int64_t>(1, (want + tiles - 1) / tiles);
+        zchunk = static_cast<int>(std::max<int64_t>(std::max(8, 4 * c.R), (nz + chunks - 1) / chunks));
+    }
+    c.zchunk = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(zchunk > 0 ? zchunk : 1, std::max<int64_t>(nz, 1))));
+    cudaError_t e = stream_dispatch(c);
+    if (e != cudaSuccess) return cuda_error(e, "streaming sweep launch");
     return UHS_OK;
+}
+
+// Read and clear the device error word after the stream drained.
+static int check_device_errors(cudaStream_t st) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    unsigned *w = device_error_word(dev);
+    if (!w) return UHS_OK;
+    unsigned h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, w, sizeof h, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "device status read");
+    if (!h) return UHS_OK;
+    cudaMemsetAsync(w, 0, sizeof(unsigned), st);
+    cudaStreamSynchronize(st);
+    if (h & kDevErrTimeout) return set_error(UHS_ETIMEOUT, "a kernel's bounded wait for its plane loads ran out");
+    return set_error(UHS_ERANGE, "a grid value is outside the float-pair range [2^-126, 2^128); "
+                                 "run this grid with UHS_ARITH_FMA");
 }
 
 static int finish(const uhs_params *p, cudaStream_t st) {
     if (p && (p->flags & UHS_FLAG_NO_SYNC)) return UHS_OK;
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_error(e, "stream synchronise");
-    return UHS_OK;
+    return check_device_errors(st);
 }
 
 static int prepare(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_memref *b, GridView *va,
@@ -243,17 +525,32 @@ int uhs_plan(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_params *p
     if (!out) return set_error(UHS_EINVAL, "out is NULL");
     SweepSpec sp;
     make_spec(d, &sp);
-    LaunchCfg cfg;
-    if ((rc = plan_cfg(sp, p, &cfg))) return rc;
-    (void)a;
+    GridView v{};
+    if (a && (rc = view_of(d, a, "a", &v))) return rc;
+    Plan pl;
+    if ((rc = plan_sweep(sp, p, v, &pl))) return rc;
     uhs_params_default(out);
-    out->kernel = cfg.kernel;
-    out->arith = cfg.arith;
-    out->tile_x = cfg.tile_x > 0 ? cfg.tile_x : 32;
-    out->tile_y = cfg.tile_y > 0 ? cfg.tile_y : 8;
-    out->tile_z = cfg.tile_z;
-    out->k_temporal = cfg.k_temporal;
-    out->use_tma = cfg.use_tma;
+    out->kernel = pl.kernel;
+    out->arith = pl.cfg.arith;
+    if (pl.kernel == UHS_KERNEL_STREAM) {
+        StreamCall c{};
+        c.shape = pl.shape;
+        c.R = pl.R;
+        c.tile = pl.tile;
+        c.ld = pl.ld;
+        int bx, by;
+        stream_tile_xy(c, &bx, &by);
+        out->tile_x = bx;
+        out->tile_y = sp.rank == 3 ? by : 1;
+        out->vy = sp.rank == 3 ? tile_shape(false, (pl.shape == kBox3 && pl.R >= 2) ? 3 : pl.tile).vy : 1;
+        out->use_tma = pl.ld == kLdTma ? 1 : -1;
+    } else {
+        out->tile_x = pl.cfg.tile_x > 0 ? pl.cfg.tile_x : 32;
+        out->tile_y = pl.cfg.tile_y > 0 ? pl.cfg.tile_y : 8;
+        out->use_tma = -1;
+    }
+    out->tile_z = pl.cfg.tile_z;
+    out->k_temporal = pl.cfg.k_temporal;
     return UHS_OK;
 }
 
@@ -264,10 +561,10 @@ int uhs_sweep(const uhs_stencil_desc *d, const uhs_memref *in, const uhs_memref 
     if (rc) return rc;
     SweepSpec sp;
     make_spec(d, &sp);
-    LaunchCfg cfg;
-    if ((rc = plan_cfg(sp, p, &cfg))) return rc;
+    Plan pl;
+    if ((rc = plan_sweep(sp, p, vi, &pl))) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if ((rc = launch_sweep(sp, cfg, vi, vo, st))) return rc;
+    if ((rc = launch_sweep(sp, pl, vi, vo, st))) return rc;
     return finish(p, st);
 }
 
@@ -278,15 +575,15 @@ int uhs_run(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_memref *b,
     if (rc) return rc;
     SweepSpec sp;
     make_spec(d, &sp);
-    LaunchCfg cfg;
-    if ((rc = plan_cfg(sp, p, &cfg))) return rc;
+    Plan pl;
+    if ((rc = plan_sweep(sp, p, va, &pl))) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (d->iterations == 1) {
-        if ((rc = launch_sweep(sp, cfg, va, vb, st))) return rc;
+        if ((rc = launch_sweep(sp, pl, va, vb, st))) return rc;
     } else {
         for (int it = 0; it < d->iterations / 2; ++it) {
-            if ((rc = launch_sweep(sp, cfg, va, vb, st))) return rc;
-            if ((rc = launch_sweep(sp, cfg, vb, va, st))) return rc;
+            if ((rc = launch_sweep(sp, pl, va, vb, st))) return rc;
+            if ((rc = launch_sweep(sp, pl, vb, va, st))) return rc;
         }
     }
     return finish(p, st);
