@@ -163,6 +163,18 @@ int uhs_sweep(const uhs_stencil_desc *desc, const uhs_memref *in, const uhs_memr
 int uhs_plan(const uhs_stencil_desc *desc, const uhs_memref *a, const uhs_params *params,
              uhs_params *out);
 
+/* FP64 error of grid x against the FP64 grid ref over desc's domain, reduced
+ * on the GPU (the comparison the reference's drivers do on the host after a
+ * run, UH-GPU/3d1r_star/3d7pt_main.cpp:84-96, here for x of any element type):
+ *   out[0] = ||x - ref||_2 / ||ref||_2    out[1] = max |x - ref|
+ *   out[2] = out[1] / max |ref|            out[3] = max |ref|
+ * x has desc->dtype (F64, F32 or F32X2 pairs); ref is F64 of the same sizes.
+ * Returns after the stream drained, with out filled.  Partial sums use
+ * scratch memory the library allocates on first use (4 doubles per 64 domain
+ * rows, grown as needed, one buffer per device, serialised by a lock). */
+int uhs_error_norms(const uhs_stencil_desc *desc, const uhs_memref *x, const uhs_memref *ref, double out[4],
+                    void *stream);
+
 /* Number of kernels this library launched since load (diagnostics). */
 int64_t uhs_launch_count(void);
 

@@ -67,6 +67,8 @@ SIGNATURES = {
     "uhs_sweep": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Memref), POINTER(Params), c_void_p]),
     "uhs_plan": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Params), POINTER(Params)]),
     "uhs_launch_count": (c_int64, []),
+    "uhs_error_norms": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Memref), POINTER(c_double),
+                                c_void_p]),
     # uhs_dsl.h
     "uhs_dsl_parse": (c_int, [c_char_p, c_char_p, POINTER(c_void_p)]),
     "uhs_program_free": (None, [c_void_p]),

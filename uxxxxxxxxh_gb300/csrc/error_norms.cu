@@ -1,0 +1,157 @@
+// FP64 error reduction on the GPU: how far a grid is from a reference grid
+// over a stencil's domain.  This is the comparison the reference's drivers
+// make on the host after every run (UH-GPU/3d1r_star/3d7pt_main.cpp:84-96,
+// |cpu - gpu| <= 1e-6 per point), done here in FP64 on the device for grids
+// of any element type so that FP32 and float-pair results can be scored
+// against an FP64 result without copying either grid back.
+//
+// Two launches: k_err_partial has each CTA reduce ERR_ROWS_PER_BLOCK rows of
+// the domain into one slot of a partials array (sum of squared differences,
+// sum of squared reference values, max |difference|, max |reference|);
+// k_err_final reduces the slots into the result.  The partials array is
+// scratch memory owned by the runtime (grown on demand, one per device).
+#include <mutex>
+
+#include "uhs_kernels.h"
+
+namespace uhs {
+int set_error(int code, const char *fmt, ...);
+
+namespace {
+
+constexpr int kErrThreads = 256;
+
+template <class T>
+__device__ __forceinline__ double load_val(const T *p);
+template <>
+__device__ __forceinline__ double load_val<double>(const double *p) {
+    return *p;
+}
+template <>
+__device__ __forceinline__ double load_val<float>(const float *p) {
+    return static_cast<double>(*p);
+}
+template <>
+__device__ __forceinline__ double load_val<float2>(const float2 *p) {
+    const float2 v = *p;
+    return static_cast<double>(v.x) + static_cast<double>(v.y);
+}
+
+struct ErrArgs {
+    const void *x;
+    const double *r;
+    int64_t xs0, xs1, rs0, rs1;
+    int64_t lb0, lb1, lb2, ub0, ub1, ub2;
+    int64_t rows;  // (ub0 - lb0) * (ub1 - lb1)
+    double *partials;
+    double *result;
+};
+
+__device__ __forceinline__ void block_reduce(double &s2, double &r2, double &md, double &mr, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) {
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+        md = fmax(md, __shfl_xor_sync(0xffffffffu, md, o));
+        mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+    }
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        sh[4 * w] = s2;
+        sh[4 * w + 1] = r2;
+        sh[4 * w + 2] = md;
+        sh[4 * w + 3] = mr;
+    }
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+        s2 = lane < nw ? sh[4 * lane] : 0.0;
+        r2 = lane < nw ? sh[4 * lane + 1] : 0.0;
+        md = lane < nw ? sh[4 * lane + 2] : 0.0;
+        mr = lane < nw ? sh[4 * lane + 3] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) {
+            s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+            r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+            md = fmax(md, __shfl_xor_sync(0xffffffffu, md, o));
+            mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+        }
+    }
+}
+
+// One CTA per ERR_ROWS_PER_BLOCK consecutive (z, y) rows of the domain.
+template <class T>
+__global__ void __launch_bounds__(kErrThreads) k_err_partial(const ErrArgs a) {
+    __shared__ double sh[4 * (kErrThreads / 32)];
+    double s2 = 0.0, r2 = 0.0, md = 0.0, mr = 0.0;
+    const int64_t ny = a.ub1 - a.lb1;
+    const int64_t row0 = static_cast<int64_t>(blockIdx.x) * kErrRowsPerBlock;
+    const int64_t row1 = min(row0 + kErrRowsPerBlock, a.rows);
+    const T *x = static_cast<const T *>(a.x);
+    for (int64_t row = row0; row < row1; ++row) {
+        const int64_t z = a.lb0 + row / ny, y = a.lb1 + row % ny;
+        const T *xr = x + z * a.xs0 + y * a.xs1;
+        const double *rr = a.r + z * a.rs0 + y * a.rs1;
+        for (int64_t i = a.lb2 + threadIdx.x; i < a.ub2; i += kErrThreads) {
+            const double rv = rr[i];
+            const double d = load_val<T>(xr + i) - rv;
+            s2 = fma(d, d, s2);
+            r2 = fma(rv, rv, r2);
+            md = fmax(md, d != d ? __longlong_as_double(0x7ff0000000000000ll) : fabs(d));
+            mr = fmax(mr, fabs(rv));
+        }
+    }
+    block_reduce(s2, r2, md, mr, sh);
+    if (threadIdx.x == 0) {
+        double *p = a.partials + 4 * static_cast<int64_t>(blockIdx.x);
+        p[0] = s2;
+        p[1] = r2;
+        p[2] = md;
+        p[3] = mr;
+    }
+}
+
+__global__ void __launch_bounds__(kErrThreads) k_err_final(const double *partials, int n, double *result) {
+    __shared__ double sh[4 * (kErrThreads / 32)];
+    double s2 = 0.0, r2 = 0.0, md = 0.0, mr = 0.0;
+    for (int i = threadIdx.x; i < n; i += kErrThreads) {
+        s2 += partials[4 * i];
+        r2 += partials[4 * i + 1];
+        md = fmax(md, partials[4 * i + 2]);
+        mr = fmax(mr, partials[4 * i + 3]);
+    }
+    block_reduce(s2, r2, md, mr, sh);
+    if (threadIdx.x == 0) {
+        result[0] = r2 > 0.0 ? sqrt(s2 / r2) : sqrt(s2);
+        result[1] = md;
+        result[2] = mr > 0.0 ? md / mr : md;
+        result[3] = mr;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_error_norms(const ErrNormsCall &c) {
+    ErrArgs a{};
+    a.x = c.x.data;
+    a.r = static_cast<const double *>(c.r.data);
+    a.xs0 = c.x.s[0];
+    a.xs1 = c.x.s[1];
+    a.rs0 = c.r.s[0];
+    a.rs1 = c.r.s[1];
+    a.lb0 = c.lb[0];
+    a.lb1 = c.lb[1];
+    a.lb2 = c.lb[2];
+    a.ub0 = c.ub[0];
+    a.ub1 = c.ub[1];
+    a.ub2 = c.ub[2];
+    a.rows = (c.ub[0] - c.lb[0]) * (c.ub[1] - c.lb[1]);
+    a.partials = c.scratch;
+    a.result = c.scratch + 4 * static_cast<int64_t>(c.nblocks);
+    if (c.dtype == UHS_F64) k_err_partial<double><<<c.nblocks, kErrThreads, 0, c.stream>>>(a);
+    else if (c.dtype == UHS_F32) k_err_partial<float><<<c.nblocks, kErrThreads, 0, c.stream>>>(a);
+    else k_err_partial<float2><<<c.nblocks, kErrThreads, 0, c.stream>>>(a);
+    k_err_final<<<1, kErrThreads, 0, c.stream>>>(a.partials, c.nblocks, a.result);
+    count_launch(2);
+    return cudaGetLastError();
+}
+
+}  // namespace uhs

@@ -46,6 +46,21 @@ unsigned *device_error_word(int device);
 cudaError_t launch_generic(const SweepSpec &sp, const LaunchCfg &cfg, const GridView &in,
                            const GridView &out, cudaStream_t st);
 
+// FP64 error reduction (error_norms.cu): one CTA per kErrRowsPerBlock rows
+// of the domain writes 4 doubles of partials into scratch; the result (4
+// doubles) follows the partials.  Scratch holds 4 * (nblocks + 1) doubles.
+constexpr int kErrRowsPerBlock = 64;
+struct ErrNormsCall {
+    int dtype;   // element type of x
+    GridView x;  // grid under test
+    GridView r;  // FP64 reference grid
+    int64_t lb[3], ub[3];
+    int nblocks;
+    double *scratch;
+    cudaStream_t stream;
+};
+cudaError_t launch_error_norms(const ErrNormsCall &c);
+
 // Launch counter shared by every launcher.
 void count_launch(int n = 1);
 

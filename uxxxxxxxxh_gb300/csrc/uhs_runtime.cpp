@@ -514,6 +514,70 @@ void uhs_params_default(uhs_params *p) {
 
 int64_t uhs_launch_count(void) { return g_launches.load(); }
 
+int uhs_error_norms(const uhs_stencil_desc *d, const uhs_memref *x, const uhs_memref *ref, double out[4],
+                    void *stream) {
+    int rc = validate_desc(d);
+    if (rc) return rc;
+    if (!out) return set_error(UHS_EINVAL, "out is NULL");
+    GridView vx, vr;
+    if ((rc = view_of(d, x, "x", &vx))) return rc;
+    uhs_stencil_desc d64 = *d;
+    d64.dtype = UHS_F64;
+    if ((rc = view_of(&d64, ref, "ref", &vr))) return rc;
+    for (int i = 0; i < 3; ++i) {
+        if (vx.n[i] != vr.n[i])
+            return set_error(UHS_EINVAL, "x and ref differ in sizes[%d] (%lld vs %lld)", i, (long long)vx.n[i],
+                             (long long)vr.n[i]);
+        if (d->lb[i] < 0 || d->ub[i] > vx.n[i])
+            return set_error(UHS_EINVAL, "domain axis %d [%lld, %lld) lies outside the grid", i, (long long)d->lb[i],
+                             (long long)d->ub[i]);
+    }
+    const int64_t rows = (d->ub[0] - d->lb[0]) * (d->ub[1] - d->lb[1]);
+    if (rows <= 0 || d->ub[2] <= d->lb[2]) {
+        out[0] = out[1] = out[2] = out[3] = 0.0;
+        return UHS_OK;
+    }
+    const int64_t nblocks = (rows + kErrRowsPerBlock - 1) / kErrRowsPerBlock;
+    if (nblocks > (int64_t(1) << 30)) return set_error(UHS_EUNSUPPORTED, "domain too large for the reduction");
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return set_error(UHS_EUNSUPPORTED, "device ordinal %d", dev);
+    // Runtime-owned scratch: one growable buffer per device, used under a lock
+    // for the whole call so concurrent callers cannot share it.
+    static std::mutex mu[64];
+    static double *buf[64] = {};
+    static int64_t cap[64] = {};
+    std::lock_guard<std::mutex> lk(mu[dev]);
+    const int64_t need = 4 * (nblocks + 1);
+    if (cap[dev] < need) {
+        if (buf[dev]) cudaFree(buf[dev]);
+        buf[dev] = nullptr;
+        cap[dev] = 0;
+        void *p = nullptr;
+        if (cudaMalloc(&p, need * sizeof(double)) != cudaSuccess)
+            return set_error(UHS_ENOMEM, "scratch allocation of %lld doubles failed", (long long)need);
+        buf[dev] = static_cast<double *>(p);
+        cap[dev] = need;
+    }
+    ErrNormsCall c{};
+    c.dtype = d->dtype;
+    c.x = vx;
+    c.r = vr;
+    for (int i = 0; i < 3; ++i) {
+        c.lb[i] = d->lb[i];
+        c.ub[i] = d->ub[i];
+    }
+    c.nblocks = static_cast<int>(nblocks);
+    c.scratch = buf[dev];
+    c.stream = static_cast<cudaStream_t>(stream);
+    cudaError_t e = launch_error_norms(c);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, c.scratch + 4 * nblocks, 4 * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) return cuda_error(e, "error-norm reduction");
+    return UHS_OK;
+}
+
 int uhs_validate(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_memref *b) {
     GridView va, vb;
     return prepare(d, a, b, &va, &vb);

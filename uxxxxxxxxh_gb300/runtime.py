@@ -118,3 +118,14 @@ def validate(stencil: Stencil, a, b) -> None:
 
 def launch_count() -> int:
     return int(_lib.lib().uhs_launch_count())
+
+
+def error_norms(stencil: Stencil, x, ref, stream=None) -> dict:
+    """FP64 error of device grid x against the FP64 device grid ref over the
+    stencil's domain, reduced on the GPU (uhs_error_norms)."""
+    d = stencil.to_desc()
+    mx = x if isinstance(x, _lib.Memref) else memref_of(x)
+    mr = ref if isinstance(ref, _lib.Memref) else memref_of(ref)
+    out = (ctypes.c_double * 4)()
+    _lib.check(_lib.lib().uhs_error_norms(d.ref(), ctypes.byref(mx), ctypes.byref(mr), out, _stream_handle(stream)))
+    return {"l2_rel": out[0], "max_abs": out[1], "max_rel": out[2], "max_ref": out[3]}
