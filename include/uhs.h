@@ -175,6 +175,30 @@ int uhs_plan(const uhs_stencil_desc *desc, const uhs_memref *a, const uhs_params
 int uhs_error_norms(const uhs_stencil_desc *desc, const uhs_memref *x, const uhs_memref *ref, double out[4],
                     void *stream);
 
+/* Partial-sum slots of the allocation-free reduction below: it accepts
+ * domains of up to UHS_NOALLOC_MAX_PARTIALS * 64 rows (a row is one (z, y)
+ * line of the domain; 524288 rows covers a 724^3 interior). */
+#define UHS_NOALLOC_MAX_PARTIALS 8192
+
+/* No counterpart in the reference.  The same reduction as uhs_error_norms
+ * (same kernels, bit-identical results) for callers that cannot allocate
+ * device memory: a plugin hosted by an application that owns every device
+ * allocation and forbids its plugins cudaMalloc, a service that must not grow
+ * its device footprint or risk an allocation failure after start-up, a
+ * latency-bound loop where cudaMalloc/cudaFree would stall on a device-wide
+ * synchronisation.  Instead of runtime-owned scratch it uses a fixed array in
+ * the library's device memory: 4 * (UHS_NOALLOC_MAX_PARTIALS + 1) doubles,
+ * 256 KiB, held on every GPU that loads the library until the process exits.
+ * A domain needing more partial slots is rejected with UHS_EUNSUPPORTED.  The
+ * call allocates and frees nothing.  Its first call on a device looks up the
+ * array's device address (a one-time set-up), so make that first call before
+ * any stream capture.  All calls on a device share the one array; each call
+ * rewrites every slot it reads, so nothing carries over between calls, but
+ * calls whose kernels overlap on the GPU (other streams, other host threads)
+ * race on it: serialise them.  Returns after the stream drained, out filled. */
+int uhs_error_norms_noalloc(const uhs_stencil_desc *desc, const uhs_memref *x, const uhs_memref *ref,
+                            double out[4], void *stream);
+
 /* Number of kernels this library launched since load (diagnostics). */
 int64_t uhs_launch_count(void);
 

@@ -1,0 +1,64 @@
+"""The allocation-free error reduction, uhs_error_norms_noalloc.
+
+Some callers of this library cannot allocate device memory: a plugin inside
+an application that owns every device allocation, a service that must not
+grow its footprint after start-up, a loop that cannot afford the device-wide
+synchronisation cudaMalloc may cause.  uhs_error_norms_noalloc serves them
+with a fixed scratch array in the library's device memory instead of the
+runtime-owned buffer uhs_error_norms allocates.  These tests call it through
+the C ABI, twice in a row on different grids (the shared array keeps the
+previous call's contents, which must not leak into the next result), and
+check each result against uhs_error_norms on the same grids.  The file is
+named so pytest collects it last.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import uxxxxxxxxh_gb300 as uhs
+from uxxxxxxxxh_gb300 import _lib
+from gpu_util import to_dev
+from uxxxxxxxxh_gb300.workloads import random_case
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def _noalloc(st, x, ref):
+    d = st.to_desc()
+    mx, mr = uhs.memref_of(x), uhs.memref_of(ref)
+    out = (ctypes.c_double * 4)()
+    rc = _lib.lib().uhs_error_norms_noalloc(d.ref(), ctypes.byref(mx), ctypes.byref(mr), out, None)
+    return rc, {"l2_rel": out[0], "max_abs": out[1], "max_rel": out[2], "max_ref": out[3]}
+
+
+def test_noalloc_matches_allocating_reduction_on_two_calls_in_a_row(cuda):
+    import torch
+    cases = [(3, (33, 41, 70), 1e-9, np.float64), (2, (257, 300), 3e-7, np.float32)]
+    for i, (rank, interior, eps, dt) in enumerate(cases):
+        st, ref = random_case(rank, 1, "box", interior, 2, 40 + i)
+        x = ref + eps * np.random.default_rng(i).standard_normal(ref.size)
+        if dt == np.float32:
+            st = st.with_(dtype=uhs.UHS_F32)
+            dx = to_dev(x.astype(np.float32), st, torch.float32)
+        else:
+            dx = to_dev(x, st)
+        dref = to_dev(ref, st)
+        rc, got = _noalloc(st, dx, dref)
+        assert rc == _lib.UHS_OK, _lib.last_error()
+        want = uhs.error_norms(st, dx, dref)
+        for k in want:
+            assert got[k] == pytest.approx(want[k], rel=TOL, abs=0.0), (i, k, got, want)
+        assert got["l2_rel"] > 0.0
+
+
+def test_noalloc_rejects_a_domain_beyond_its_scratch(cuda):
+    rows = _lib.UHS_NOALLOC_MAX_PARTIALS * 64 + 1
+    st, _ = random_case(2, 1, "star", (rows, 2), 2, 3)
+    import torch
+    g = torch.zeros(st.sizes[1:], dtype=torch.float64, device="cuda")
+    rc, _ = _noalloc(st, g, g.clone())
+    assert rc == _lib.UHS_EUNSUPPORTED
+    assert "partial slots" in _lib.last_error()

@@ -27,6 +27,7 @@ UHS_KERNEL_AUTO, UHS_KERNEL_GENERIC, UHS_KERNEL_STREAM, UHS_KERNEL_MMA = 0, 1, 2
 UHS_FLAG_NO_SYNC, UHS_FLAG_NO_TUNE_DB = 1, 2
 
 UHS_MAX_TERMS = 512
+UHS_NOALLOC_MAX_PARTIALS = 8192
 UHS_MAX_RADIUS = 4
 
 
@@ -69,6 +70,8 @@ SIGNATURES = {
     "uhs_launch_count": (c_int64, []),
     "uhs_error_norms": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Memref), POINTER(c_double),
                                 c_void_p]),
+    "uhs_error_norms_noalloc": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Memref),
+                                        POINTER(c_double), c_void_p]),
     # uhs_dsl.h
     "uhs_dsl_parse": (c_int, [c_char_p, c_char_p, POINTER(c_void_p)]),
     "uhs_program_free": (None, [c_void_p]),

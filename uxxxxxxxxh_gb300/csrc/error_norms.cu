@@ -14,8 +14,17 @@
 
 #include "uhs_kernels.h"
 
+// Scratch of uhs_error_norms_noalloc: partial sums of up to
+// UHS_NOALLOC_MAX_PARTIALS CTAs plus the 4-double result.  Lives in the
+// library's device memory on every GPU that loads it; host code must not use
+// this name as an address (it is a host-side stand-in): the device address
+// comes from cudaGetSymbolAddress below.
+static __device__ __align__(256) double g_noalloc_scratch[4 * (UHS_NOALLOC_MAX_PARTIALS + 1)];
+
 namespace uhs {
 int set_error(int code, const char *fmt, ...);
+int prepare_error_norms(const uhs_stencil_desc *d, const uhs_memref *x, const uhs_memref *ref, ErrNormsCall *c,
+                        bool *empty);
 
 namespace {
 
@@ -155,3 +164,58 @@ cudaError_t launch_error_norms(const ErrNormsCall &c) {
 }
 
 }  // namespace uhs
+
+// One-time set-up per device, with that device current: the device address
+// of g_noalloc_scratch.  Returns nullptr (and sets the error) on failure.
+static double *noalloc_scratch(int dev) {
+    static std::mutex mu;
+    static double *addr[64] = {};
+    if (dev < 0 || dev >= 64) {
+        uhs::set_error(UHS_EUNSUPPORTED, "device ordinal %d is beyond the 64 this library tracks", dev);
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) {
+            uhs::set_error(UHS_ECUDA, "cudaGetSymbolAddress of the reduction scratch: %s", cudaGetErrorString(e));
+            return nullptr;
+        }
+        addr[dev] = static_cast<double *>(p);
+    }
+    return addr[dev];
+}
+
+extern "C" int uhs_error_norms_noalloc(const uhs_stencil_desc *d, const uhs_memref *x, const uhs_memref *ref,
+                                       double out[4], void *stream) {
+    uhs::ErrNormsCall c;
+    bool empty = false;
+    int rc = uhs::prepare_error_norms(d, x, ref, &c, &empty);
+    if (rc) return rc;
+    if (!out) return uhs::set_error(UHS_EINVAL, "out is NULL");
+    if (empty) {
+        out[0] = out[1] = out[2] = out[3] = 0.0;
+        return UHS_OK;
+    }
+    if (c.nblocks > UHS_NOALLOC_MAX_PARTIALS)
+        return uhs::set_error(UHS_EUNSUPPORTED,
+                              "the domain has %lld rows and needs %d partial slots; the allocation-free reduction "
+                              "holds %d (domains of up to %d rows): use uhs_error_norms",
+                              (long long)((d->ub[0] - d->lb[0]) * (d->ub[1] - d->lb[1])), c.nblocks,
+                              UHS_NOALLOC_MAX_PARTIALS, UHS_NOALLOC_MAX_PARTIALS * uhs::kErrRowsPerBlock);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return uhs::set_error(UHS_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+    double *scratch = noalloc_scratch(dev);
+    if (!scratch) return UHS_ECUDA;
+    c.scratch = scratch;
+    c.stream = static_cast<cudaStream_t>(stream);
+    e = uhs::launch_error_norms(c);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, scratch + 4 * static_cast<int64_t>(c.nblocks), 4 * sizeof(double),
+                            cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) return uhs::set_error(UHS_ECUDA, "allocation-free error reduction: %s", cudaGetErrorString(e));
+    return UHS_OK;
+}

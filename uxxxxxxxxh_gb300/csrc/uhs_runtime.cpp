@@ -498,6 +498,40 @@ static int prepare(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_mem
     return check_reach(d, *va);
 }
 
+// Validation and launch description shared by error-reduction entry points
+// that bring their own scratch (the caller fills c->scratch and c->stream).
+int prepare_error_norms(const uhs_stencil_desc *d, const uhs_memref *x, const uhs_memref *ref, ErrNormsCall *c,
+                        bool *empty) {
+    int rc = validate_desc(d);
+    if (rc) return rc;
+    GridView vx, vr;
+    if ((rc = view_of(d, x, "x", &vx))) return rc;
+    uhs_stencil_desc d64 = *d;
+    d64.dtype = UHS_F64;
+    if ((rc = view_of(&d64, ref, "ref", &vr))) return rc;
+    for (int i = 0; i < 3; ++i) {
+        if (vx.n[i] != vr.n[i])
+            return set_error(UHS_EINVAL, "x and ref differ in sizes[%d] (%lld vs %lld)", i, (long long)vx.n[i],
+                             (long long)vr.n[i]);
+        if (d->lb[i] < 0 || d->ub[i] > vx.n[i])
+            return set_error(UHS_EINVAL, "domain axis %d [%lld, %lld) lies outside the grid", i, (long long)d->lb[i],
+                             (long long)d->ub[i]);
+    }
+    const int64_t rows = (d->ub[0] - d->lb[0]) * (d->ub[1] - d->lb[1]);
+    *empty = rows <= 0 || d->ub[2] <= d->lb[2];
+    std::memset(c, 0, sizeof *c);
+    c->dtype = d->dtype;
+    c->x = vx;
+    c->r = vr;
+    for (int i = 0; i < 3; ++i) {
+        c->lb[i] = d->lb[i];
+        c->ub[i] = d->ub[i];
+    }
+    const int64_t nblocks = *empty ? 0 : (rows + kErrRowsPerBlock - 1) / kErrRowsPerBlock;
+    c->nblocks = static_cast<int>(std::min<int64_t>(nblocks, int64_t(1) << 30));
+    return UHS_OK;
+}
+
 }  // namespace uhs
 
 using namespace uhs;
