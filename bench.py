@@ -228,10 +228,14 @@ def main():
     ms_step = ms / args.steps
     plan = uhs.plan(st, dev_a, params)
 
-    # Roofline of the sweep kernel: algorithmic bytes per launch / avg launch time.
+    # Roofline of the sweep kernel: algorithmic bytes per launch / avg launch
+    # time.  A step launches T sweeps (plus, under UHS_ARITH_AUTO on FP64, two
+    # short range scans); the whole step time is charged to the sweeps, so the
+    # achieved bandwidth is a slight underestimate.
     eb = st.elem_bytes
     launches_per_step = max(1, launches // max(1, args.steps))
-    avg_launch_s = (ms * 1e-3) / max(1, launches)
+    sweeps = st.iterations * args.steps
+    avg_launch_s = (ms * 1e-3) / max(1, sweeps)
     alg_bytes = 2 * eb * st.interior_points
     peak, peak_kind = load_peaks()
     achieved = alg_bytes / avg_launch_s / 1e9
@@ -320,6 +324,7 @@ def main():
                      "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_launch_s * 1e3},
         "gpu_launches": launches,
         "launches_per_step": launches_per_step,
+        "sweep_launches": sweeps,
         "clocks": clk,
         "e2e": e2e,
         "cpu_baseline": cpu,

@@ -55,7 +55,10 @@ enum {
 };
 
 enum {
-    UHS_ARITH_AUTO = 0,  /* the backend picks (fastest mode within 1e-12 for F64) */
+    UHS_ARITH_AUTO = 0,  /* the backend picks: for F64 grids on the streaming kernel,
+                            UHS_ARITH_DF32 when a device scan of both grids shows
+                            max|x| * (sum|c|)^T < 2^119 (one extra read of each grid
+                            and one host round trip per call), else UHS_ARITH_FMA */
     UHS_ARITH_FMA = 1,   /* native arithmetic, products fused into the sum */
     UHS_ARITH_EXACT = 2, /* separately rounded products and sums in expression
                             order: bit-identical to the serial CPU loops */

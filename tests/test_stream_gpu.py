@@ -150,3 +150,34 @@ def test_forced_tma_on_unaligned_rows_is_refused(cuda):
     with pytest.raises(uhs.UhsError) as ei:
         run_gpu(st, a0, uhs.RunParams(kernel=STREAM, use_tma=1))
     assert ei.value.code == uhs._lib.UHS_EUNSUPPORTED
+
+
+def test_auto_arithmetic_uses_float_pairs_and_falls_back_on_range(cuda):
+    st, a0 = _case(3, 1, "star", T=4, interior=(12, 20, 40))
+    assert uhs.plan(st).arith == uhs.UHS_ARITH_DF32
+    ra, _ = run_oracle(st, a0)
+    ga, _ = run_gpu(st, a0)  # UHS_ARITH_AUTO
+    assert_f64_close(st, ra, ga)
+    # a value near the float-pair limit: AUTO must run native FP64 instead of failing
+    a1 = a0.copy()
+    a1[len(a1) // 2] = 1e36
+    ra1, _ = run_oracle(st, a1)
+    ga1, _ = run_gpu(st, a1)
+    assert_f64_close(st, ra1, ga1)
+    # growth bound: coefficients summing to 2.8 over T = 200 steps exceed 2^128
+    st2 = st.with_(terms=[(t[0], t[1], t[2], 0.4) for t in st.terms], iterations=2)
+    ra2, _ = run_oracle(st2, a0)
+    ga2, _ = run_gpu(st2, a0)
+    assert_f64_close(st2, ra2, ga2)
+
+
+def test_f32_pair_loads_and_single_loads_agree(cuda):
+    """Even pitches take the 8-byte cp.async path, odd ones the 4-byte path."""
+    import torch
+    for interior in [(9, 20, 64), (9, 20, 63)]:
+        st, a0 = _case(3, 2, "star", T=2, interior=interior)
+        st32 = st.with_(dtype=uhs.UHS_F32)
+        a32 = a0.astype(np.float32)
+        ra, _ = run_oracle(st, a32.astype(np.float64))
+        ga, _ = run_gpu(st32, a32, uhs.RunParams(kernel=STREAM, use_tma=-1), dtype=torch.float32)
+        assert oracle.error(st, ra, ga)["l2_rel"] <= 1e-6

@@ -23,6 +23,7 @@ struct StreamCall {
     int64_t lb[3], ub[3];
     const CUtensorMap *tmap;
     int shift;
+    int pair_loads;
     unsigned *err;
     cudaStream_t stream;
     int *occ_out;  // when set: report CTAs per SM of the variant instead of launching

@@ -105,7 +105,8 @@ struct StreamArgs {
     int64_t n0, n1, n2;
     int64_t lb0, lb1, lb2, ub0, ub1, ub2;
     int zchunk;
-    int shift;  // TMA box starts this many elements left of x0 - R (16-byte granule)
+    int shift;       // TMA box starts this many elements left of x0 - R (16-byte granule)
+    int pair_loads;  // cp.async of 4-byte elements in 8-byte pairs (origin and pitches even)
     unsigned *err;
     double cd[NT];
     float ch[NT], cl[NT];
@@ -251,14 +252,30 @@ __global__ void __launch_bounds__(C::THREADS) k_stream(const __grid_constant__ S
         if constexpr (C::LD == kLdCpAsync) {
             const TS *plane = static_cast<const TS *>(a.in) + p * a.in_s0;
             TS *dst = stg_base + slot * STG_ELEMS;
+            if (C::EB == 4 && a.pair_loads) {
+                // 8-byte granules: thread tx copies columns 2tx, 2tx+1 (W is even).
+                constexpr int NPAIR = (BX + 2 * R + 1) / 2;
+                const int gxp = static_cast<int>(gx0) + 2 * tx;
+                const bool pok = tx < NPAIR && gxp + 1 < a.n2;
 #pragma unroll
-            for (int i = 0; i < NLOAD_ROWS; ++i) {
-                const int r = ty + i * TYT;
-                if (r < H) {
-                    const TS *src = plane + row_off[i];
-                    cp_async<C::EB>(dst + r * W + tx, row_ok[i] && col_a ? src + gxa : plane, row_ok[i] && col_a);
-                    if (tx < 2 * R) cp_async<C::EB>(dst + r * W + tx + BX, row_ok[i] && col_b ? src + gxb : plane,
-                                                    row_ok[i] && col_b);
+                for (int i = 0; i < NLOAD_ROWS; ++i) {
+                    const int r = ty + i * TYT;
+                    if (r < H && tx < NPAIR) {
+                        const bool ok = row_ok[i] && pok;
+                        cp_async<8>(dst + r * W + 2 * tx, ok ? plane + row_off[i] + gxp : plane, ok);
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < NLOAD_ROWS; ++i) {
+                    const int r = ty + i * TYT;
+                    if (r < H) {
+                        const TS *src = plane + row_off[i];
+                        cp_async<C::EB>(dst + r * W + tx, row_ok[i] && col_a ? src + gxa : plane, row_ok[i] && col_a);
+                        if (tx < 2 * R)
+                            cp_async<C::EB>(dst + r * W + tx + BX, row_ok[i] && col_b ? src + gxb : plane,
+                                            row_ok[i] && col_b);
+                    }
                 }
             }
         } else {

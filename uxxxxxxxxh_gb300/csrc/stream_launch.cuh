@@ -31,6 +31,7 @@ cudaError_t launch_cfg(const StreamCall &c) {
     a.ub2 = c.ub[2];
     a.zchunk = c.zchunk;
     a.shift = c.shift;
+    a.pair_loads = c.pair_loads;
     a.err = c.err;
     for (int k = 0; k < C::NT; ++k) {
         const double v = c.coef[k];

@@ -1,6 +1,7 @@
 // Internal interface between the host runtime (uhs_runtime.cpp) and the sweep
 // kernels (*.cu).  Not part of the C ABI.
 #pragma once
+#include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
 #include "../../include/uhs.h"
@@ -60,6 +61,10 @@ struct ErrNormsCall {
     cudaStream_t stream;
 };
 cudaError_t launch_error_norms(const ErrNormsCall &c);
+
+// Max of the biased exponent fields of n_words doubles into *out (atomicMax;
+// *out must start at 0).
+cudaError_t launch_max_exponent(const void *data, int64_t n_words, unsigned *out, int sms, cudaStream_t st);
 
 // Launch counter shared by every launcher.
 void count_launch(int n = 1);

@@ -21,6 +21,7 @@
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -55,8 +56,9 @@ unsigned *device_error_word(int device) {
     std::lock_guard<std::mutex> lk(mu);
     if (!words[device]) {
         void *p = nullptr;
-        if (cudaMalloc(&p, sizeof(unsigned)) != cudaSuccess) return nullptr;
-        cudaMemset(p, 0, sizeof(unsigned));
+        // word 0: kernel status flags; word 1: range-scan result
+        if (cudaMalloc(&p, 2 * sizeof(unsigned)) != cudaSuccess) return nullptr;
+        cudaMemset(p, 0, 2 * sizeof(unsigned));
         words[device] = static_cast<unsigned *>(p);
     }
     return words[device];
@@ -178,6 +180,7 @@ struct Plan {
     // streaming kernel
     int shape = -1, R = 0, st = 0, ar = 0, ld = kLdCpAsync, tile = 0, zchunk = 0;
     std::vector<double> coef;  // coef_slot order
+    bool auto_df32 = false;    // df32 chosen by UHS_ARITH_AUTO, subject to range_ok()
 };
 
 static int device_sms() {
@@ -257,7 +260,16 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
     int shape = -1, R = 0;
     const bool shaped = classify(sp, &shape, &R);
     int arith = p->arith;
-    if (arith == UHS_ARITH_AUTO) arith = sp.dtype == UHS_F32X2 ? UHS_ARITH_DF32 : UHS_ARITH_FMA;
+    pl->auto_df32 = false;
+    if (arith == UHS_ARITH_AUTO) {
+        if (sp.dtype == UHS_F32X2) arith = UHS_ARITH_DF32;
+        else if (sp.dtype == UHS_F64 && shaped) {
+            // FP64 on the streaming kernel: float pairs unless the range check
+            // in range_ok() vetoes them for this run's data.
+            arith = UHS_ARITH_DF32;
+            pl->auto_df32 = true;
+        } else arith = UHS_ARITH_FMA;
+    }
     if (sp.dtype == UHS_F32 && arith == UHS_ARITH_DF32)
         return set_error(UHS_EUNSUPPORTED, "float-pair arithmetic needs F64 or F32X2 grids");
     if (sp.dtype == UHS_F32X2 && arith != UHS_ARITH_DF32)
@@ -294,6 +306,9 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
         else if (cfg.tile_x == 256) tile = 2;
         else if (cfg.tile_x != 0 && cfg.tile_x != 128)
             return set_error(UHS_EINVAL, "rank-2 streaming tiles are 64, 128 or 256 wide (got %d)", cfg.tile_x);
+    } else if (cfg.tile_x == 0 && cfg.tile_y == 0 && p->vy == 0) {
+        // measured on GB300 (3d7pt, 512^3): df32 fastest at 64 x 8, native FP32 at 32 x 32
+        tile = arith == UHS_ARITH_DF32 ? 2 : 0;
     } else {
         if (cfg.tile_x == 64) tile = 2;
         else if (cfg.tile_x != 0 && cfg.tile_x != 32)
@@ -396,6 +411,31 @@ static GridView kernel_view(const SweepSpec &sp, const GridView &v) {
     return k;
 }
 
+// UHS_ARITH_AUTO on FP64 grids: float pairs represent magnitudes below 2^128.
+// Scan both grids for their largest exponent and bound the growth over T
+// sweeps by (sum |c|)^T; fall back to native FP64 when the bound comes within
+// 2^8 of the limit, or when a grid holds Inf/NaN.
+static bool range_ok(const SweepSpec &sp, const GridView &a, const GridView &b, int T, cudaStream_t st) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    unsigned *w = device_error_word(dev);
+    if (!w) return false;
+    unsigned *scan = w + 1;
+    if (cudaMemsetAsync(scan, 0, sizeof(unsigned), st) != cudaSuccess) return false;
+    for (const GridView *g : {&a, &b}) {
+        const int64_t span = (g->n[0] - 1) * g->s[0] + (g->n[1] - 1) * g->s[1] + g->n[2];
+        if (launch_max_exponent(g->data, span, scan, device_sms(), st) != cudaSuccess) return false;
+    }
+    unsigned e = 0;
+    if (cudaMemcpyAsync(&e, scan, sizeof e, cudaMemcpyDeviceToHost, st) != cudaSuccess) return false;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return false;
+    if (e >= 0x7ffu) return false;  // Inf or NaN somewhere
+    double csum = 0.0;
+    for (int k = 0; k < sp.nterms; ++k) csum += std::fabs(sp.coef[k]);
+    const double growth = csum > 1.0 ? std::max(T, 1) * std::log2(csum) : 0.0;
+    return static_cast<double>(static_cast<int>(e) - 1023) + 1.0 + growth < 120.0;
+}
+
 static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in, const GridView &out,
                         cudaStream_t st) {
     if (pl.kernel == UHS_KERNEL_GENERIC) {
@@ -454,6 +494,12 @@ static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in,
         zchunk = static_cast<int>(std::max<int64_t>(std::max(8, 4 * c.R), (nz + chunks - 1) / chunks));
     }
     c.zchunk = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(zchunk > 0 ? zchunk : 1, std::max<int64_t>(nz, 1))));
+    // 4-byte grids: copy in 8-byte pairs when every row start of the tile is 8-byte aligned
+    if (eb == 4 && c.ld == kLdCpAsync) {
+        const bool even = ((c.lb[2] - c.R) % 2 == 0) && c.in.s[0] % 2 == 0 && c.in.s[1] % 2 == 0 &&
+                          c.in.n[2] % 2 == 0 && reinterpret_cast<uintptr_t>(c.in.data) % 8 == 0;
+        c.pair_loads = even ? 1 : 0;
+    }
     cudaError_t e = stream_dispatch(c);
     if (e != cudaSuccess) return cuda_error(e, "streaming sweep launch");
     return UHS_OK;
@@ -662,6 +708,10 @@ int uhs_sweep(const uhs_stencil_desc *d, const uhs_memref *in, const uhs_memref 
     Plan pl;
     if ((rc = plan_sweep(sp, p, vi, &pl))) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (pl.auto_df32 && !range_ok(sp, vi, vo, 1, st)) {
+        pl.ar = kArNative;
+        pl.cfg.arith = UHS_ARITH_FMA;
+    }
     if ((rc = launch_sweep(sp, pl, vi, vo, st))) return rc;
     return finish(p, st);
 }
@@ -676,6 +726,10 @@ int uhs_run(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_memref *b,
     Plan pl;
     if ((rc = plan_sweep(sp, p, va, &pl))) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (pl.auto_df32 && d->iterations > 0 && !range_ok(sp, va, vb, d->iterations, st)) {
+        pl.ar = kArNative;
+        pl.cfg.arith = UHS_ARITH_FMA;
+    }
     if (d->iterations == 1) {
         if ((rc = launch_sweep(sp, pl, va, vb, st))) return rc;
     } else {
