@@ -202,6 +202,32 @@ int uhs_error_norms(const uhs_stencil_desc *desc, const uhs_memref *x, const uhs
 int uhs_error_norms_noalloc(const uhs_stencil_desc *desc, const uhs_memref *x, const uhs_memref *ref,
                             double out[4], void *stream);
 
+/* ---- batches: many programs advanced together -------------------------- */
+/* A batch runs n programs (each its own grids a[i], b[i], descriptor and T)
+ * with one persistent kernel launch per timestep: every grid is cut into
+ * tiles x z-chunks, and the launch's CTAs walk the combined list, each item
+ * swept by its grid's variant (star/box, radius 1-3, rank 2/3, FP64 in float
+ * pairs or native, FP32).  uhs_batch_create plans the batch, uploads the
+ * per-grid arguments, and captures the whole timestep loop (max T launches;
+ * a program stops after its own T) into a CUDA graph; uhs_batch_run replays
+ * it on a stream.  Programs the streaming kernels do not cover (generic
+ * shapes, UHS_ARITH_EXACT) are rejected with UHS_EUNSUPPORTED.  The grids
+ * must stay allocated for the batch's lifetime.  params (may be NULL) applies
+ * to every program; only its arith field is used. */
+typedef struct uhs_batch uhs_batch;
+
+int uhs_batch_create(const uhs_stencil_desc *descs, const uhs_memref *a, const uhs_memref *b, int32_t n,
+                     const uhs_params *params, uhs_batch **out);
+/* Replay the captured timestep loop on stream; synchronous unless flags has
+ * UHS_FLAG_NO_SYNC. */
+int uhs_batch_run(uhs_batch *batch, void *stream, int32_t flags);
+/* Launches per replay, timesteps, work items per timestep (first step). */
+int uhs_batch_stats(const uhs_batch *batch, int64_t *launches, int64_t *steps, int64_t *items);
+void uhs_batch_destroy(uhs_batch *batch);
+/* create + run + destroy */
+int uhs_run_batch(const uhs_stencil_desc *descs, const uhs_memref *a, const uhs_memref *b, int32_t n,
+                  const uhs_params *params, void *stream);
+
 /* Number of kernels this library launched since load (diagnostics). */
 int64_t uhs_launch_count(void);
 

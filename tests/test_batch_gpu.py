@@ -1,0 +1,95 @@
+"""Batches: many programs advanced by one persistent launch per timestep,
+the timestep loop replayed from a CUDA graph.  Every grid of the batch must
+match its own oracle run (FP64 within 1e-12, FP32 within a relative L2 of
+1e-6), whatever mix of shapes, precisions, extents and T shares the batch."""
+import numpy as np
+import pytest
+
+import oracle
+import uxxxxxxxxh_gb300 as uhs
+from gpu_util import assert_f64_close, run_oracle, to_dev
+from uxxxxxxxxh_gb300.workloads import cfg5_specs, random_case
+
+pytestmark = pytest.mark.gpu
+
+
+def _grids(specs):
+    import torch
+    devs_a, devs_b, host = [], [], []
+    for st, seed in specs:
+        a0 = 2.0 * uhs.workloads.splitmix_uniform(seed, int(np.prod(st.sizes))) - 1.0
+        if st.dtype == uhs.UHS_F32:
+            a0 = a0.astype(np.float32).astype(np.float64)
+            d = to_dev(a0.astype(np.float32), st, torch.float32)
+        else:
+            d = to_dev(a0, st)
+        devs_a.append(d)
+        devs_b.append(d.clone())
+        host.append(a0)
+    return devs_a, devs_b, host
+
+
+def _check(specs, devs_a, devs_b, host):
+    for (st, _), da, db, a0 in zip(specs, devs_a, devs_b, host):
+        ra, rb = run_oracle(st, a0)
+        ga = da.cpu().numpy().reshape(-1).astype(np.float64)
+        gb = db.cpu().numpy().reshape(-1).astype(np.float64)
+        if st.dtype == uhs.UHS_F32:
+            assert oracle.error(st, ra, ga)["l2_rel"] <= 1e-6, st.name
+            if st.iterations > 1:
+                assert oracle.error(st, rb, gb)["l2_rel"] <= 1e-6, st.name
+        else:
+            assert_f64_close(st, ra, ga)
+            assert_f64_close(st, rb, gb)
+
+
+def test_mixed_batch_matches_oracle(cuda):
+    specs = cfg5_specs(n_grids=24, T=4, seed=11, side2=(40, 300), side3=(12, 48))
+    kinds = {(st.rank, st.radius[2], st.nterms, st.dtype) for st, _ in specs}
+    assert len(kinds) >= 10
+    a, b, host = _grids(specs)
+    batch = uhs.Batch([s for s, _ in specs], a, b)
+    stats = batch.stats()
+    assert stats["steps"] == 4 and stats["launches"] >= 4
+    batch.run()
+    _check(specs, a, b, host)
+    batch.close()
+
+
+def test_batch_with_different_iteration_counts_and_replay(cuda):
+    specs = cfg5_specs(n_grids=9, T=4, seed=12, side2=(50, 200), side3=(10, 30))
+    Ts = [4, 2, 1, 6, 4, 2, 0, 4, 2]
+    specs = [(st.with_(iterations=t), sd) for (st, sd), t in zip(specs, Ts)]
+    a, b, host = _grids(specs)
+    batch = uhs.Batch([s for s, _ in specs], a, b)
+    assert batch.stats()["steps"] == 6
+    batch.run()
+    _check(specs, a, b, host)
+    # a second replay continues from the first run's result
+    batch.run()
+    for (st, _), da, a0 in zip(specs, a, host):
+        if st.iterations == 0 or st.dtype == uhs.UHS_F32 or st.iterations == 1:
+            continue
+        r1, r1b = run_oracle(st, a0)
+        r2, _ = run_oracle(st, r1, r1b)
+        assert_f64_close(st, r2, da.cpu().numpy().reshape(-1))
+    batch.close()
+
+
+def test_one_launch_per_timestep_for_a_mixed_precision_batch(cuda):
+    specs = cfg5_specs(n_grids=12, T=6, seed=13, side2=(64, 128), side3=(16, 24))
+    a, b, _ = _grids(specs)
+    batch = uhs.Batch([s for s, _ in specs], a, b)
+    n0 = uhs.launch_count()
+    batch.run()
+    assert batch.stats()["launches"] == 6
+    assert uhs.launch_count() - n0 == 6
+
+
+def test_batch_rejects_programs_outside_the_streaming_kernels(cuda):
+    st, a0 = random_case(3, 1, "star", (8, 8, 8), 2, 1)
+    odd = st.with_(terms=st.terms + [(1, 1, 0, 0.01)])  # not a star, not a full box
+    a = to_dev(a0, st)
+    with pytest.raises(uhs.UhsError):
+        uhs.Batch([st, st.with_(terms=[(0, 0, 0, 1.0)])], [a, a.clone()], [a.clone(), a.clone()])
+    del odd

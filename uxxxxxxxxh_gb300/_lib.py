@@ -68,6 +68,13 @@ SIGNATURES = {
     "uhs_sweep": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Memref), POINTER(Params), c_void_p]),
     "uhs_plan": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Params), POINTER(Params)]),
     "uhs_launch_count": (c_int64, []),
+    "uhs_batch_create": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Memref), c_int32, POINTER(Params),
+                                 POINTER(c_void_p)]),
+    "uhs_batch_run": (c_int, [c_void_p, c_void_p, c_int32]),
+    "uhs_batch_stats": (c_int, [c_void_p, POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)]),
+    "uhs_batch_destroy": (None, [c_void_p]),
+    "uhs_run_batch": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Memref), c_int32, POINTER(Params),
+                              c_void_p]),
     "uhs_error_norms": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Memref), POINTER(c_double),
                                 c_void_p]),
     "uhs_error_norms_noalloc": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Memref),

@@ -12,8 +12,26 @@ enum { kStar3 = 0, kBox3 = 1, kStar2 = 2, kBox2 = 3 };
 enum { kStF64 = 0, kStF32 = 1, kStF32x2 = 2 };
 enum { kArNative = 0, kArDf32 = 1 };
 enum { kLdCpAsync = 0, kLdTma = 1 };
+// Term capacity of a batched grid's arguments (the 7x7x7 box).
+constexpr int kBatchNT = 343;
 
 constexpr int ct_round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+template <int NT>
+struct StreamArgs {
+    CUtensorMap tmap;  // TMA loader only
+    const void *in;
+    void *out;
+    int64_t in_s0, in_s1, out_s0, out_s1;
+    int64_t n0, n1, n2;
+    int64_t lb0, lb1, lb2, ub0, ub1, ub2;
+    int zchunk;
+    int shift;       // TMA box starts this many elements left of x0 - R (16-byte granule)
+    int pair_loads;  // cp.async of 4-byte elements in 8-byte pairs (origin and pitches even)
+    unsigned *err;
+    double cd[NT];
+    float ch[NT], cl[NT];
+};
 
 // Everything one streaming launch needs (filled by the runtime).
 struct StreamCall {
@@ -73,5 +91,37 @@ inline void stream_tile_xy(const StreamCall &c, int *bx, int *by) {
     *bx = big_box ? 32 : t.bx;
     *by = big_box ? 16 : t.tyt * t.vy;
 }
+
+}  // namespace uhs
+
+namespace uhs {
+
+// ---- batched persistent launches (stream_batch.cu) ----------------------
+// Every grid of a batch carries its arguments at the largest term count
+// (343, the 7x7x7 box), once per ping-pong direction, and the index of its
+// variant inside the persistent kernel's variant pack.
+// A distinct type (not an alias of StreamArgs<343>): the kernels read a
+// BatchArgs from shared memory, a StreamArgs from the parameter bank, and
+// choose their coefficient loads by this type.
+struct BatchArgs : StreamArgs<kBatchNT> {};
+struct alignas(64) BatchGrid {
+    BatchArgs dir[2];  // [0]: a -> b, [1]: b -> a
+    int kind;
+};
+// Packs: 0 = float-pair FP64 and native FP32 variants of all 12 shapes (one
+// launch per step covers a mixed FP32/FP64 batch); 1 = native FP64.
+enum { kPackMain = 0, kPackF64Native = 1, kNumPacks = 2 };
+struct BatchPackInfo {
+    int smem, threads, occ;
+};
+// Variant index of (shape, R, storage, arithmetic) in a pack, or -1.
+int batch_kind(int pack, int shape, int R, int st, int ar);
+// Tile and z-chunk every batch item of that variant uses.
+void batch_tile(int shape, int R, int *bx, int *by, int *zchunk);
+cudaError_t batch_prepare(int pack, BatchPackInfo *info);
+cudaError_t batch_launch(int pack, const BatchGrid *grids, const int4 *items, int n_items, int dir, int ctas,
+                         cudaStream_t st);
+// Host-side packing of one direction's arguments (coefficients in slot order).
+void batch_fill_args(BatchArgs *a, const StreamCall &c, int nt);
 
 }  // namespace uhs

@@ -96,21 +96,6 @@ struct StreamCfg {
     static_assert(!SI::is2d || (TYT == 1 && VY == 1), "rank-2 tiles are one row");
 };
 
-template <int NT>
-struct StreamArgs {
-    CUtensorMap tmap;  // TMA loader only
-    const void *in;
-    void *out;
-    int64_t in_s0, in_s1, out_s0, out_s1;
-    int64_t n0, n1, n2;
-    int64_t lb0, lb1, lb2, ub0, ub1, ub2;
-    int zchunk;
-    int shift;       // TMA box starts this many elements left of x0 - R (16-byte granule)
-    int pair_loads;  // cp.async of 4-byte elements in 8-byte pairs (origin and pitches even)
-    unsigned *err;
-    double cd[NT];
-    float ch[NT], cl[NT];
-};
 
 // ---- asynchronous copy primitives --------------------------------------
 template <int BYTES>
@@ -161,6 +146,33 @@ __device__ __forceinline__ void tma_load_3d(void *smem, const CUtensorMap *map, 
 }
 
 // ---- arithmetic policies -----------------------------------------------
+// Coefficient reads.  Kernel parameters (StreamArgs) sit in the constant
+// bank and feed the FMA directly.  The batched kernel keeps each item's
+// arguments in shared memory (BatchArgs); for stencils of more than
+// 32 terms it reads every coefficient where it is used, through a volatile
+// load the compiler cannot hoist out of the plane loop (hoisting 343 of them
+// would exhaust the register file).
+template <class C, class Args>
+__device__ __forceinline__ double coef_d(const Args &a, int k) {
+    if constexpr (std::is_same_v<Args, BatchArgs> && (C::NT > 32)) {
+        double v;
+        asm volatile("ld.shared.f64 %0, [%1];" : "=d"(v) : "r"((unsigned)__cvta_generic_to_shared(&a.cd[k])));
+        return v;
+    } else {
+        return a.cd[k];
+    }
+}
+template <class C, class Args>
+__device__ __forceinline__ float coef_f(const Args &a, const float *p) {
+    if constexpr (std::is_same_v<Args, BatchArgs> && (C::NT > 32)) {
+        float v;
+        asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"((unsigned)__cvta_generic_to_shared(p)));
+        return v;
+    } else {
+        return *p;
+    }
+}
+
 template <class C, int AR = C::AR>
 struct Arith;
 
@@ -168,14 +180,17 @@ template <class C>
 struct Arith<C, kArNative> {
     using TS = typename C::TS;
     using Acc = TS;
-    __device__ static __forceinline__ TS coef(const StreamArgs<C::NT> &a, int k) {
-        if constexpr (std::is_same_v<TS, double>) return a.cd[k];
-        else return a.ch[k];
+    template <class Args>
+    __device__ static __forceinline__ TS coef(const Args &a, int k) {
+        if constexpr (std::is_same_v<TS, double>) return coef_d<C>(a, k);
+        else return coef_f<C>(a, &a.ch[k]);
     }
-    __device__ static __forceinline__ void first(Acc &acc, const StreamArgs<C::NT> &a, int k, TS v) {
+    template <class Args>
+    __device__ static __forceinline__ void first(Acc &acc, const Args &a, int k, TS v) {
         acc = coef(a, k) * v;
     }
-    __device__ static __forceinline__ void add(Acc &acc, const StreamArgs<C::NT> &a, int k, TS v) {
+    template <class Args>
+    __device__ static __forceinline__ void add(Acc &acc, const Args &a, int k, TS v) {
         acc = fma(coef(a, k), v, acc);
     }
     __device__ static __forceinline__ void store(TS *p, const Acc &acc) { *p = acc; }
@@ -184,11 +199,13 @@ struct Arith<C, kArNative> {
 template <class C>
 struct Arith<C, kArDf32> {
     using Acc = df;
-    __device__ static __forceinline__ void first(Acc &acc, const StreamArgs<C::NT> &a, int k, float2 v) {
-        df_mul(acc, a.ch[k], a.cl[k], v);
+    template <class Args>
+    __device__ static __forceinline__ void first(Acc &acc, const Args &a, int k, float2 v) {
+        df_mul(acc, coef_f<C>(a, &a.ch[k]), coef_f<C>(a, &a.cl[k]), v);
     }
-    __device__ static __forceinline__ void add(Acc &acc, const StreamArgs<C::NT> &a, int k, float2 v) {
-        df_fma(acc, a.ch[k], a.cl[k], v);
+    template <class Args>
+    __device__ static __forceinline__ void add(Acc &acc, const Args &a, int k, float2 v) {
+        df_fma(acc, coef_f<C>(a, &a.ch[k]), coef_f<C>(a, &a.cl[k]), v);
     }
     __device__ static __forceinline__ void store(typename C::TS *p, const Acc &acc) {
         if constexpr (C::ST == kStF64) *p = join_f64(acc.h, acc.l);
@@ -197,8 +214,12 @@ struct Arith<C, kArDf32> {
 };
 
 // ---- the kernel ---------------------------------------------------------
-template <class C>
-__global__ void __launch_bounds__(C::THREADS) k_stream(const __grid_constant__ StreamArgs<C::NT> a) {
+// One work item: the (bx, by) tile of the (y, x) plane over z-chunk bz.
+// Returns false when a bounded wait ran out (the status word is set).
+// Leaves no copy in flight and ends with a barrier, so a persistent caller can
+// start its next item on the same shared memory right away.
+template <class C, class Args>
+__device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int bzi, unsigned char *smem) {
     using TS = typename C::TS;
     using TC = typename C::TC;
     using A = Arith<C>;
@@ -208,12 +229,14 @@ __global__ void __launch_bounds__(C::THREADS) k_stream(const __grid_constant__ S
     constexpr int STG_ELEMS = C::STG_SLOT / C::EB, CMP_ELEMS = C::CMP_SLOT / (int)sizeof(TC);
     constexpr bool STAR = C::SI::star, IS2D = C::SI::is2d;
     constexpr int NLOAD_ROWS = (H + TYT - 1) / TYT;  // cp.async: rows per thread
-    extern __shared__ __align__(128) unsigned char smem[];
 
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
-    const int64_t x0 = a.lb2 + static_cast<int64_t>(blockIdx.x) * BX;
-    const int64_t y0 = a.lb1 + static_cast<int64_t>(blockIdx.y) * C::BY;
-    const int64_t zs = a.lb0 + static_cast<int64_t>(blockIdx.z) * a.zchunk;
+    // Thread coordinates from the linear index, so a caller launched with
+    // another 256-thread block shape (the batched kernel) maps the same way.
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int tx = tid % BX, ty = tid / BX;
+    const int64_t x0 = a.lb2 + static_cast<int64_t>(bxi) * BX;
+    const int64_t y0 = a.lb1 + static_cast<int64_t>(byi) * C::BY;
+    const int64_t zs = a.lb0 + static_cast<int64_t>(bzi) * a.zchunk;
     const int64_t ze = min(zs + static_cast<int64_t>(a.zchunk), a.ub0);
     const int64_t gx0 = x0 - R - a.shift, gy0 = y0 - RY;
     const int64_t qbeg = zs - R;
@@ -223,14 +246,6 @@ __global__ void __launch_bounds__(C::THREADS) k_stream(const __grid_constant__ S
     uint64_t *const mbar = reinterpret_cast<uint64_t *>(smem + NSTG * C::STG_SLOT + (C::CONVERT ? NCMP * C::CMP_SLOT : 0));
     constexpr int CMP_STRIDE = C::CONVERT ? CMP_ELEMS : STG_ELEMS;
     constexpr int NRING = C::CONVERT ? NCMP : NSTG;  // ring the compute reads
-
-    if constexpr (C::LD == kLdTma) {
-        if (tid == 0) {
-            for (int s = 0; s < NSTG; ++s) mbar_init(mbar + s, 1);
-            asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-        }
-        __syncthreads();
-    }
 
     // cp.async: per-thread row offsets inside a plane (32-bit: a plane holds
     // fewer than 2^31 elements, which the host checks) and validity.
@@ -322,7 +337,7 @@ __global__ void __launch_bounds__(C::THREADS) k_stream(const __grid_constant__ S
                     for (int k = j; k < min(j + PD, nq); ++k)
                         (void)mbar_wait(mbar + (k % NSTG), static_cast<unsigned>((k / NSTG) & 1));
                 }
-                return;
+                return false;
             }
         }
         if (j + PD < nq) issue(j + PD, s_iss);
@@ -434,6 +449,23 @@ __global__ void __launch_bounds__(C::THREADS) k_stream(const __grid_constant__ S
     if constexpr (C::CONVERT) {
         if (range_err) atomicOr(a.err, kDevErrRange);
     }
+    __syncthreads();
+    return true;
+}
+
+template <class C>
+__global__ void __launch_bounds__(C::THREADS) k_stream(const __grid_constant__ StreamArgs<C::NT> a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    if constexpr (C::LD == kLdTma) {
+        uint64_t *const mbar = reinterpret_cast<uint64_t *>(smem + C::NSTG * C::STG_SLOT +
+                                                            (C::CONVERT ? C::NCMP * C::CMP_SLOT : 0));
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            for (int s = 0; s < C::NSTG; ++s) mbar_init(mbar + s, 1);
+            asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        }
+        __syncthreads();
+    }
+    (void)stream_item<C>(a, blockIdx.x, blockIdx.y, blockIdx.z, smem);
 }
 
 }  // namespace uhs

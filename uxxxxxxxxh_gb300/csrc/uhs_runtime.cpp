@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <map>
+#include <memory>
 #include <tuple>
 #include <atomic>
 #include <cstdarg>
@@ -578,6 +579,200 @@ int prepare_error_norms(const uhs_stencil_desc *d, const uhs_memref *x, const uh
     return UHS_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// Batches (stream_batch.cu): one persistent launch per timestep, replayed
+// from a CUDA graph.
+// ---------------------------------------------------------------------------
+struct BatchGridHost {
+    int pack, kind, T, order;
+    int64_t items;
+};
+
+struct uhs_batch_impl {
+    int dev = 0;
+    int n = 0;
+    int steps = 0;
+    int64_t launches = 0, items0 = 0;
+    BatchGrid *d_grids = nullptr;
+    int4 *d_items[kNumPacks] = {nullptr, nullptr};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+static void batch_free(uhs_batch_impl *b) {
+    if (!b) return;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->d_grids) cudaFree(b->d_grids);
+    for (auto *p : b->d_items)
+        if (p) cudaFree(p);
+    delete b;
+}
+
+static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, const uhs_memref *bs, int32_t n,
+                        const uhs_params *params, uhs_batch_impl **out) {
+    if (!descs || !as || !bs || !out || n < 0) return set_error(UHS_EINVAL, "batch arguments must be non-NULL");
+    auto *B = new uhs_batch_impl();
+    std::unique_ptr<uhs_batch_impl, void (*)(uhs_batch_impl *)> guard(B, batch_free);
+    cudaGetDevice(&B->dev);
+    B->n = n;
+    std::vector<BatchGrid> host(static_cast<size_t>(n));
+    std::vector<BatchGridHost> info(static_cast<size_t>(n));
+    std::vector<std::vector<int4>> items(kNumPacks);
+    unsigned *err = device_error_word(B->dev);
+    if (!err) return set_error(UHS_ENOMEM, "device status word allocation failed");
+    cudaStream_t scan_stream = nullptr;
+    if (cudaStreamCreateWithFlags(&scan_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return set_error(UHS_ECUDA, "stream creation failed");
+    struct StreamGuard {
+        cudaStream_t s;
+        ~StreamGuard() { cudaStreamDestroy(s); }
+    } sg{scan_stream};
+    for (int32_t i = 0; i < n; ++i) {
+        GridView va, vb;
+        int rc = prepare(&descs[i], &as[i], &bs[i], &va, &vb);
+        if (rc) return set_error(rc, "program %d: %s", i, uhs_last_error());
+        SweepSpec sp;
+        make_spec(&descs[i], &sp);
+        Plan pl;
+        if ((rc = plan_sweep(sp, params, va, &pl))) return set_error(rc, "program %d: %s", i, uhs_last_error());
+        if (pl.kernel != UHS_KERNEL_STREAM)
+            return set_error(UHS_EUNSUPPORTED, "program %d is not a star/box stencil the batched kernel covers", i);
+        if (pl.auto_df32 && descs[i].iterations > 0 && !range_ok(sp, va, vb, descs[i].iterations, scan_stream)) {
+            pl.ar = kArNative;
+            pl.cfg.arith = UHS_ARITH_FMA;
+        }
+        int pack = kPackMain, kind = batch_kind(kPackMain, pl.shape, pl.R, pl.st, pl.ar);
+        if (kind < 0) {
+            pack = kPackF64Native;
+            kind = batch_kind(pack, pl.shape, pl.R, pl.st, pl.ar);
+        }
+        if (kind < 0) return set_error(UHS_EUNSUPPORTED, "program %d: no batched variant for its element type", i);
+        StreamCall c{};
+        c.shape = pl.shape;
+        c.R = pl.R;
+        c.st = pl.st;
+        c.ar = pl.ar;
+        c.ld = kLdCpAsync;
+        c.coef = pl.coef.data();
+        const bool is2d = sp.rank == 2;
+        c.lb[0] = is2d ? sp.lb[1] : sp.lb[0];
+        c.ub[0] = is2d ? sp.ub[1] : sp.ub[0];
+        c.lb[1] = is2d ? 0 : sp.lb[1];
+        c.ub[1] = is2d ? 1 : sp.ub[1];
+        c.lb[2] = sp.lb[2];
+        c.ub[2] = sp.ub[2];
+        c.err = err;
+        int bx, by, zc;
+        batch_tile(pl.shape, pl.R, &bx, &by, &zc);
+        c.zchunk = zc;
+        const int eb = sp.dtype == UHS_F32 ? 4 : 8;
+        for (int d = 0; d < 2; ++d) {
+            c.in = kernel_view(sp, d == 0 ? va : vb);
+            c.out = kernel_view(sp, d == 0 ? vb : va);
+            c.pair_loads = 0;
+            if (eb == 4)
+                c.pair_loads = ((c.lb[2] - c.R) % 2 == 0) && c.in.s[0] % 2 == 0 && c.in.s[1] % 2 == 0 &&
+                               c.in.n[2] % 2 == 0 && reinterpret_cast<uintptr_t>(c.in.data) % 8 == 0;
+            batch_fill_args(&host[i].dir[d], c, static_cast<int>(pl.coef.size()));
+        }
+        host[i].kind = kind;
+        const int64_t tx = (c.ub[2] - c.lb[2] + bx - 1) / bx, ty = (c.ub[1] - c.lb[1] + by - 1) / by,
+                      tz = (c.ub[0] - c.lb[0] + zc - 1) / zc;
+        info[i] = BatchGridHost{pack, kind, descs[i].iterations, i, tx * ty * tz};
+        if (tx * ty * tz > (int64_t(1) << 28)) return set_error(UHS_EUNSUPPORTED, "program %d has too many tiles", i);
+    }
+    // Items of each pack, grids in decreasing T so a timestep's active items
+    // are a prefix of the list.
+    std::vector<int> order(static_cast<size_t>(n));
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return info[x].T > info[y].T; });
+    std::vector<std::vector<int64_t>> prefix(kNumPacks);  // prefix[pack][step] = active items
+    int steps = 0;
+    for (int i = 0; i < n; ++i) steps = std::max(steps, info[i].T);
+    B->steps = steps;
+    for (int p = 0; p < kNumPacks; ++p) prefix[p].assign(static_cast<size_t>(steps), 0);
+    for (int i : order) {
+        const int p = info[i].pack;
+        GridView dummy{};
+        (void)dummy;
+        int bx, by, zc;
+        SweepSpec sp;
+        make_spec(&descs[i], &sp);
+        int shape = -1, R = 0;
+        classify(sp, &shape, &R);
+        batch_tile(shape, R, &bx, &by, &zc);
+        const BatchArgs &a0 = host[i].dir[0];
+        const int64_t tx = (a0.ub2 - a0.lb2 + bx - 1) / bx, ty = (a0.ub1 - a0.lb1 + by - 1) / by,
+                      tz = (a0.ub0 - a0.lb0 + zc - 1) / zc;
+        for (int64_t z = 0; z < tz; ++z)
+            for (int64_t y = 0; y < ty; ++y)
+                for (int64_t x = 0; x < tx; ++x)
+                    items[p].push_back(make_int4(i, static_cast<int>(x), static_cast<int>(y), static_cast<int>(z)));
+        for (int s = 0; s < info[i].T; ++s) prefix[p][s] = static_cast<int64_t>(items[p].size());
+    }
+    if (items[0].size() + items[1].size() > static_cast<size_t>(INT32_MAX))
+        return set_error(UHS_EUNSUPPORTED, "batch has too many work items");
+    // Upload.
+    if (n > 0) {
+        void *p = nullptr;
+        if (cudaMalloc(&p, sizeof(BatchGrid) * static_cast<size_t>(n)) != cudaSuccess)
+            return set_error(UHS_ENOMEM, "batch argument upload: allocation failed");
+        B->d_grids = static_cast<BatchGrid *>(p);
+        if (cudaMemcpy(B->d_grids, host.data(), sizeof(BatchGrid) * static_cast<size_t>(n), cudaMemcpyHostToDevice) !=
+            cudaSuccess)
+            return set_error(UHS_ECUDA, "batch argument upload failed");
+    }
+    int ctas[kNumPacks] = {0, 0};
+    for (int p = 0; p < kNumPacks; ++p) {
+        if (items[p].empty()) continue;
+        void *q = nullptr;
+        if (cudaMalloc(&q, sizeof(int4) * items[p].size()) != cudaSuccess)
+            return set_error(UHS_ENOMEM, "batch item list: allocation failed");
+        B->d_items[p] = static_cast<int4 *>(q);
+        if (cudaMemcpy(q, items[p].data(), sizeof(int4) * items[p].size(), cudaMemcpyHostToDevice) != cudaSuccess)
+            return set_error(UHS_ECUDA, "batch item upload failed");
+        BatchPackInfo bi;
+        cudaError_t e = batch_prepare(p, &bi);
+        if (e != cudaSuccess) return cuda_error(e, "batch kernel set-up");
+        const int64_t want = static_cast<int64_t>(device_sms()) * std::max(1, bi.occ);
+        ctas[p] = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(want, static_cast<int64_t>(items[p].size()))));
+    }
+    B->items0 = 0;
+    for (int p = 0; p < kNumPacks; ++p)
+        if (steps > 0) B->items0 += prefix[p][0];
+    // Capture the timestep loop.
+    if (steps > 0) {
+        cudaStream_t cs;
+        if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
+            return set_error(UHS_ECUDA, "capture stream creation failed");
+        StreamGuard cg{cs};
+        if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+            return set_error(UHS_ECUDA, "graph capture could not start");
+        cudaError_t e = cudaSuccess;
+        int64_t launches = 0;
+        for (int s = 0; s < steps && e == cudaSuccess; ++s) {
+            for (int p = 0; p < kNumPacks && e == cudaSuccess; ++p) {
+                const int64_t m = prefix[p][s];
+                if (m <= 0) continue;
+                e = batch_launch(p, B->d_grids, B->d_items[p], static_cast<int>(m), s & 1, ctas[p], cs);
+                ++launches;
+            }
+        }
+        cudaGraph_t g = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return cuda_error(e != cudaSuccess ? e : e2, "batch graph capture");
+        }
+        B->graph = g;
+        if ((e = cudaGraphInstantiate(&B->exec, g, 0)) != cudaSuccess) return cuda_error(e, "batch graph instantiate");
+        B->launches = launches;
+    }
+    *out = guard.release();
+    return UHS_OK;
+}
 }  // namespace uhs
 
 using namespace uhs;
@@ -739,6 +934,59 @@ int uhs_run(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_memref *b,
         }
     }
     return finish(p, st);
+}
+
+struct uhs_batch {
+    uhs_batch_impl *impl;
+};
+
+int uhs_batch_create(const uhs_stencil_desc *descs, const uhs_memref *a, const uhs_memref *b, int32_t n,
+                     const uhs_params *params, uhs_batch **out) {
+    if (!out) return set_error(UHS_EINVAL, "out is NULL");
+    *out = nullptr;
+    uhs_batch_impl *impl = nullptr;
+    int rc = batch_create(descs, a, b, n, params, &impl);
+    if (rc) return rc;
+    *out = new uhs_batch{impl};
+    return UHS_OK;
+}
+
+int uhs_batch_run(uhs_batch *batch, void *stream, int32_t flags) {
+    if (!batch || !batch->impl) return set_error(UHS_EINVAL, "batch is NULL");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (batch->impl->exec) {
+        cudaError_t e = cudaGraphLaunch(batch->impl->exec, st);
+        if (e != cudaSuccess) return cuda_error(e, "batch graph launch");
+        count_launch(static_cast<int>(batch->impl->launches));
+    }
+    uhs_params p;
+    uhs_params_default(&p);
+    p.flags = flags;
+    return finish(&p, st);
+}
+
+int uhs_batch_stats(const uhs_batch *batch, int64_t *launches, int64_t *steps, int64_t *items) {
+    if (!batch || !batch->impl) return set_error(UHS_EINVAL, "batch is NULL");
+    if (launches) *launches = batch->impl->launches;
+    if (steps) *steps = batch->impl->steps;
+    if (items) *items = batch->impl->items0;
+    return UHS_OK;
+}
+
+void uhs_batch_destroy(uhs_batch *batch) {
+    if (!batch) return;
+    batch_free(batch->impl);
+    delete batch;
+}
+
+int uhs_run_batch(const uhs_stencil_desc *descs, const uhs_memref *a, const uhs_memref *b, int32_t n,
+                  const uhs_params *params, void *stream) {
+    uhs_batch *bt = nullptr;
+    int rc = uhs_batch_create(descs, a, b, n, params, &bt);
+    if (rc) return rc;
+    rc = uhs_batch_run(bt, stream, params ? params->flags & ~UHS_FLAG_NO_SYNC : 0);
+    uhs_batch_destroy(bt);
+    return rc;
 }
 
 }  // extern "C"

@@ -129,3 +129,39 @@ def error_norms(stencil: Stencil, x, ref, stream=None) -> dict:
     out = (ctypes.c_double * 4)()
     _lib.check(_lib.lib().uhs_error_norms(d.ref(), ctypes.byref(mx), ctypes.byref(mr), out, _stream_handle(stream)))
     return {"l2_rel": out[0], "max_abs": out[1], "max_rel": out[2], "max_ref": out[3]}
+
+
+class Batch:
+    """Many programs advanced together: one persistent launch per timestep,
+    the timestep loop replayed from a CUDA graph (uhs_batch_*)."""
+
+    def __init__(self, stencils, grids_a, grids_b, params: RunParams | None = None):
+        n = len(stencils)
+        self._holders = [s.to_desc() for s in stencils]
+        self._descs = (_lib.StencilDesc * n)(*[h.desc for h in self._holders])
+        self._a = (_lib.Memref * n)(*[g if isinstance(g, _lib.Memref) else memref_of(g) for g in grids_a])
+        self._b = (_lib.Memref * n)(*[g if isinstance(g, _lib.Memref) else memref_of(g) for g in grids_b])
+        self._keep = (grids_a, grids_b)
+        p = (params or RunParams()).to_c()
+        self._h = ctypes.c_void_p()
+        _lib.check(_lib.lib().uhs_batch_create(self._descs, self._a, self._b, n, ctypes.byref(p),
+                                               ctypes.byref(self._h)))
+
+    def run(self, stream=None, sync: bool = True) -> None:
+        _lib.check(_lib.lib().uhs_batch_run(self._h, _stream_handle(stream), 0 if sync else _lib.UHS_FLAG_NO_SYNC))
+
+    def stats(self) -> dict:
+        l, s, i = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _lib.check(_lib.lib().uhs_batch_stats(self._h, ctypes.byref(l), ctypes.byref(s), ctypes.byref(i)))
+        return {"launches": l.value, "steps": s.value, "items": i.value}
+
+    def close(self) -> None:
+        if self._h:
+            _lib.lib().uhs_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -114,3 +114,28 @@ def random_case(rank: int, r: int, kind: str, interior, T: int, seed: int, dtype
     st = make_stencil(f"{rank}d{r}r_{kind}", rank, interior, r, offs, coefs, iterations=T, dtype=dtype)
     a = 2.0 * splitmix_uniform(seed, int(np.prod(st.sizes))) - 1.0
     return st, a
+
+
+def cfg5_specs(n_grids: int = 64, T: int = 20, seed: int = 5, side2=(256, 8192), side3=(64, 512)):
+    """The batched mixed suite: n_grids programs drawn from the seed, each one
+    of the 12 shapes ({2d,3d} x {r1,r2,r3} x {star,box}) in FP32 or FP64,
+    2D sides log-uniform in side2, 3D sides log-uniform in side3 (each axis
+    drawn separately, so grids are not cubic), normalised U[0,1) coefficients.
+    Returns [(Stencil, data seed)]; data is U[-1,1) from that seed."""
+    from ._lib import UHS_F32
+    u = splitmix_uniform(seed, n_grids * 8)
+    out = []
+    for g in range(n_grids):
+        v = u[8 * g: 8 * g + 8]
+        shape = min(11, int(v[0] * 12))
+        rank = 2 if shape < 6 else 3
+        kind = "star" if shape % 2 == 0 else "box"
+        r = 1 + (shape // 2) % 3
+        lo, hi = side2 if rank == 2 else side3
+        sides = [int(round(math.exp(math.log(lo) + x * (math.log(hi) - math.log(lo))))) for x in v[1:1 + rank]]
+        dtype = UHS_F32 if v[4] < 0.5 else UHS_F64
+        offs = star_offsets(rank, r) if kind == "star" else box_offsets(rank, r)
+        coefs = normalised(splitmix_uniform(seed * 1000 + g, len(offs)) + 0.05)
+        st = make_stencil(f"g{g}_{rank}d{r}r_{kind}", rank, sides, r, offs, coefs, iterations=T, dtype=dtype)
+        out.append((st, seed * 7919 + g))
+    return out
