@@ -228,6 +228,43 @@ void uhs_batch_destroy(uhs_batch *batch);
 int uhs_run_batch(const uhs_stencil_desc *descs, const uhs_memref *a, const uhs_memref *b, int32_t n,
                   const uhs_params *params, void *stream);
 
+/* ---- tuner database ------------------------------------------------------ */
+/* The planner's first source of launch parameters.  Entries are keyed by the
+ * program's shape class (rank, star or box, radius), element type and domain
+ * extents.  A uhs_run / uhs_sweep whose params are NULL or all zero apart from
+ * flags, without UHS_FLAG_NO_TUNE_DB, takes the entry with its exact key, else
+ * the entry of the same class and element type nearest in log2 extents, else
+ * the planner's defaults.  An entry's float-pair arithmetic is applied as
+ * UHS_ARITH_AUTO, so the range check still guards it.  Filled by the tuner
+ * (uxxxxxxxxh_gb300/tuner.py, exhaustive search) or the learned cost model. */
+int uhs_tune_put(const uhs_stencil_desc *desc, const uhs_params *best, double gstencil_per_s);
+/* The parameters the database would give desc (UHS_EINVAL when it has none
+ * for the class); *exact is set to 1 for an exact-key hit. */
+int uhs_tune_get(const uhs_stencil_desc *desc, uhs_params *out, int32_t *exact);
+void uhs_tune_clear(void);
+int64_t uhs_tune_size(void);
+
+/* ---- learned cost model --------------------------------------------------- */
+/* A small MLP (in_dim -> hidden x layers (ReLU) -> 1) trained and evaluated by
+ * the library's own GPU kernels; the tuner uses it to rank launch candidates
+ * of programs it has not timed (uxxxxxxxxh_gb300/costmodel.py).  Parameters
+ * are one flat float array, layer by layer [W (out x in, row-major), b (out)].
+ * Training minimises the mean squared error with Adam on minibatches drawn by
+ * a seeded permutation of a data set copied to the device once. */
+typedef struct uhs_mlp uhs_mlp;
+int uhs_mlp_create(int32_t in_dim, int32_t hidden, int32_t layers, uint64_t seed, uhs_mlp **out);
+void uhs_mlp_destroy(uhs_mlp *m);
+int64_t uhs_mlp_num_params(const uhs_mlp *m);
+int uhs_mlp_get_params(const uhs_mlp *m, float *out);
+int uhs_mlp_set_params(uhs_mlp *m, const float *in);
+/* y[i] = net(x[i]) for n rows of in_dim floats (host arrays). */
+int uhs_mlp_forward(uhs_mlp *m, const float *x, int32_t n, float *y);
+/* Mean squared error of the n rows against y and its gradient with respect
+ * to every parameter (host arrays; grad has uhs_mlp_num_params entries). */
+int uhs_mlp_loss_grad(uhs_mlp *m, const float *x, const float *y, int32_t n, float *loss, float *grad);
+int uhs_mlp_train(uhs_mlp *m, const float *x, const float *y, int32_t n, int32_t epochs, int32_t batch, float lr,
+                  uint64_t seed, float *final_loss);
+
 /* Number of kernels this library launched since load (diagnostics). */
 int64_t uhs_launch_count(void);
 

@@ -68,6 +68,20 @@ SIGNATURES = {
     "uhs_sweep": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Memref), POINTER(Params), c_void_p]),
     "uhs_plan": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Params), POINTER(Params)]),
     "uhs_launch_count": (c_int64, []),
+    "uhs_mlp_create": (c_int, [c_int32, c_int32, c_int32, ctypes.c_uint64, POINTER(c_void_p)]),
+    "uhs_mlp_destroy": (None, [c_void_p]),
+    "uhs_mlp_num_params": (c_int64, [c_void_p]),
+    "uhs_mlp_get_params": (c_int, [c_void_p, POINTER(ctypes.c_float)]),
+    "uhs_mlp_set_params": (c_int, [c_void_p, POINTER(ctypes.c_float)]),
+    "uhs_mlp_forward": (c_int, [c_void_p, POINTER(ctypes.c_float), c_int32, POINTER(ctypes.c_float)]),
+    "uhs_mlp_loss_grad": (c_int, [c_void_p, POINTER(ctypes.c_float), POINTER(ctypes.c_float), c_int32,
+                                  POINTER(ctypes.c_float), POINTER(ctypes.c_float)]),
+    "uhs_mlp_train": (c_int, [c_void_p, POINTER(ctypes.c_float), POINTER(ctypes.c_float), c_int32, c_int32, c_int32,
+                              ctypes.c_float, ctypes.c_uint64, POINTER(ctypes.c_float)]),
+    "uhs_tune_put": (c_int, [POINTER(StencilDesc), POINTER(Params), c_double]),
+    "uhs_tune_get": (c_int, [POINTER(StencilDesc), POINTER(Params), POINTER(c_int32)]),
+    "uhs_tune_clear": (None, []),
+    "uhs_tune_size": (c_int64, []),
     "uhs_batch_create": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Memref), c_int32, POINTER(Params),
                                  POINTER(c_void_p)]),
     "uhs_batch_run": (c_int, [c_void_p, c_void_p, c_int32]),

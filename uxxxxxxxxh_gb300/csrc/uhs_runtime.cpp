@@ -773,6 +773,85 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
     *out = guard.release();
     return UHS_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Tuner database (include/uhs.h): best launch parameters per program class.
+// ---------------------------------------------------------------------------
+struct TuneKey {
+    int rank, shape, R, dtype;
+    int64_t ext[3];
+    bool operator<(const TuneKey &o) const {
+        return std::tie(rank, shape, R, dtype, ext[0], ext[1], ext[2]) <
+               std::tie(o.rank, o.shape, o.R, o.dtype, o.ext[0], o.ext[1], o.ext[2]);
+    }
+};
+struct TuneEntry {
+    uhs_params p;
+    double gst;
+};
+static std::mutex g_tune_mu;
+static std::map<TuneKey, TuneEntry> g_tune;
+
+static bool tune_key(const uhs_stencil_desc *d, TuneKey *k) {
+    SweepSpec sp;
+    make_spec(d, &sp);
+    int shape = -1, R = 0;
+    if (!classify(sp, &shape, &R)) return false;
+    k->rank = d->rank;
+    k->shape = shape;
+    k->R = R;
+    k->dtype = d->dtype;
+    for (int i = 0; i < 3; ++i) k->ext[i] = d->ub[i] - d->lb[i];
+    return true;
+}
+
+static bool tune_lookup(const uhs_stencil_desc *d, uhs_params *out, bool *exact) {
+    TuneKey k;
+    if (!tune_key(d, &k)) return false;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(k);
+    if (it != g_tune.end()) {
+        *out = it->second.p;
+        *exact = true;
+        return true;
+    }
+    double best = 1e300;
+    const TuneEntry *hit = nullptr;
+    for (const auto &kv : g_tune) {
+        const TuneKey &e = kv.first;
+        if (e.rank != k.rank || e.shape != k.shape || e.R != k.R || e.dtype != k.dtype) continue;
+        double dist = 0.0;
+        for (int i = 0; i < 3; ++i)
+            dist += std::fabs(std::log2(static_cast<double>(std::max<int64_t>(1, e.ext[i]))) -
+                              std::log2(static_cast<double>(std::max<int64_t>(1, k.ext[i]))));
+        if (dist < best) {
+            best = dist;
+            hit = &kv.second;
+        }
+    }
+    if (!hit) return false;
+    *out = hit->p;
+    *exact = false;
+    return true;
+}
+
+static bool params_are_auto(const uhs_params *p) {
+    if (!p) return true;
+    return p->kernel == 0 && p->arith == 0 && p->tile_x == 0 && p->tile_y == 0 && p->tile_z == 0 &&
+           p->k_temporal == 0 && p->use_tma == 0 && p->vy == 0 && p->prefetch == 0;
+}
+
+// The parameters a call runs with: the caller's, or the database's when the
+// caller left everything on auto.
+static const uhs_params *effective_params(const uhs_stencil_desc *d, const uhs_params *p, uhs_params *buf) {
+    if (!params_are_auto(p) || (p && (p->flags & UHS_FLAG_NO_TUNE_DB))) return p;
+    if (validate_desc(d) != UHS_OK) return p;  // the caller's own validation reports it
+    bool exact = false;
+    if (!tune_lookup(d, buf, &exact)) return p;
+    if (buf->arith == UHS_ARITH_DF32) buf->arith = UHS_ARITH_AUTO;
+    buf->flags = p ? p->flags : 0;
+    return buf;
+}
 }  // namespace uhs
 
 using namespace uhs;
@@ -861,6 +940,8 @@ int uhs_validate(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_memre
 int uhs_plan(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_params *p, uhs_params *out) {
     int rc = validate_desc(d);
     if (rc) return rc;
+    uhs_params tuned;
+    p = effective_params(d, p, &tuned);
     if (!out) return set_error(UHS_EINVAL, "out is NULL");
     SweepSpec sp;
     make_spec(d, &sp);
@@ -895,6 +976,8 @@ int uhs_plan(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_params *p
 
 int uhs_sweep(const uhs_stencil_desc *d, const uhs_memref *in, const uhs_memref *out, const uhs_params *p,
               void *stream) {
+    uhs_params tuned;
+    if (d) p = effective_params(d, p, &tuned);
     GridView vi, vo;
     int rc = prepare(d, in, out, &vi, &vo);
     if (rc) return rc;
@@ -913,6 +996,8 @@ int uhs_sweep(const uhs_stencil_desc *d, const uhs_memref *in, const uhs_memref 
 
 int uhs_run(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_memref *b, const uhs_params *p,
             void *stream) {
+    uhs_params tuned;
+    if (d) p = effective_params(d, p, &tuned);
     GridView va, vb;
     int rc = prepare(d, a, b, &va, &vb);
     if (rc) return rc;
@@ -987,6 +1072,37 @@ int uhs_run_batch(const uhs_stencil_desc *descs, const uhs_memref *a, const uhs_
     rc = uhs_batch_run(bt, stream, params ? params->flags & ~UHS_FLAG_NO_SYNC : 0);
     uhs_batch_destroy(bt);
     return rc;
+}
+
+int uhs_tune_put(const uhs_stencil_desc *d, const uhs_params *best, double gst) {
+    int rc = validate_desc(d);
+    if (rc) return rc;
+    if (!best) return set_error(UHS_EINVAL, "best is NULL");
+    TuneKey k;
+    if (!tune_key(d, &k)) return set_error(UHS_EUNSUPPORTED, "only star and box programs of radius 1-3 are tuned");
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[k] = TuneEntry{*best, gst};
+    return UHS_OK;
+}
+
+int uhs_tune_get(const uhs_stencil_desc *d, uhs_params *out, int32_t *exact) {
+    int rc = validate_desc(d);
+    if (rc) return rc;
+    if (!out) return set_error(UHS_EINVAL, "out is NULL");
+    bool ex = false;
+    if (!tune_lookup(d, out, &ex)) return set_error(UHS_EINVAL, "the tuner database has no entry for this class");
+    if (exact) *exact = ex ? 1 : 0;
+    return UHS_OK;
+}
+
+void uhs_tune_clear(void) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune.clear();
+}
+
+int64_t uhs_tune_size(void) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    return static_cast<int64_t>(g_tune.size());
 }
 
 }  // extern "C"

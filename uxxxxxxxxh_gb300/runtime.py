@@ -103,7 +103,7 @@ def plan(stencil: Stencil, a=None, params: RunParams | None = None) -> RunParams
     d = stencil.to_desc()
     out = _lib.Params()
     p = (params or RunParams()).to_c()
-    ma = memref_of(a) if a is not None else None
+    ma = (a if isinstance(a, _lib.Memref) else memref_of(a)) if a is not None else None
     _lib.check(_lib.lib().uhs_plan(d.ref(), ctypes.byref(ma) if ma is not None else None, ctypes.byref(p),
                                    ctypes.byref(out)))
     return RunParams.from_c(out)

@@ -1,0 +1,208 @@
+"""Exhaustive autotuner for the streaming sweep.
+
+UHStencil searches its compile-time tiling space at random
+(scripts/evaluation_scripts_GPU/test_driver.py:169-285: grid/block tile
+sizes, inner tile, shared-memory flag; 1000 random configurations, each
+compiled and timed with nsys) and keeps the fastest per case
+(collect.py:384-419).  Here the same knobs are run-time parameters of one
+library, so the search is exhaustive and cheap: every candidate is timed with
+CUDA events on device-resident grids, and the winner goes into the library's
+tuner database (uhs_tune_put), which the planner consults whenever a caller
+leaves the parameters on auto.  Every timing is also kept as a training
+record for the learned cost model (costmodel.py).
+
+Candidates (rank 3): tile {32x32 VY4, 32x16 VY4, 64x8 VY2, 32x16 VY2} x
+loader {TMA, cp.async} x z-chunk {auto, 16, 64} x arithmetic (FP64:
+{float pairs, native}); rank 2: rows {64, 128, 256} x loader x z-chunk
+{auto, 128, 512} x arithmetic; plus the generic kernel.  Candidates that plan
+to the same launch are timed once.
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import math
+import os
+from dataclasses import asdict
+
+from . import _lib
+from .runtime import RunParams, memref_of, memref_raw, plan
+from .stencil import Stencil
+
+STREAM, GENERIC = _lib.UHS_KERNEL_STREAM, _lib.UHS_KERNEL_GENERIC
+TILES3 = [(32, 32, 4), (32, 16, 4), (64, 8, 2), (32, 16, 2)]
+TILES2 = [64, 128, 256]
+
+
+def class_features(st: Stencil) -> list:
+    """Program features: rank, radius, box, FP64, log2 extents, log2 terms."""
+    rz, ry, rx = st.radius
+    r = max(rz, ry, rx)
+    box = any(sum(1 for v in t[:3] if v != 0) > 1 for t in st.terms)
+    ext = [max(1, u - l) for l, u in zip(st.lb, st.ub)]
+    return [1.0 if st.rank == 3 else 0.0, r / 3.0, 1.0 if box else 0.0, 1.0 if st.dtype != _lib.UHS_F32 else 0.0,
+            math.log2(ext[0]) / 10.0, math.log2(ext[1]) / 10.0, math.log2(ext[2]) / 13.0,
+            math.log2(len(st.terms)) / 9.0]
+
+
+def config_features(p: RunParams) -> list:
+    """Launch features of a planned configuration."""
+    tile = [0.0] * 7
+    if p.kernel == STREAM:
+        if p.tile_y > 1:
+            key = (p.tile_x, p.tile_y, p.vy)
+            if key in TILES3:
+                tile[TILES3.index(key)] = 1.0
+        elif p.tile_x in TILES2:
+            tile[4 + TILES2.index(p.tile_x)] = 1.0
+    return tile + [1.0 if p.use_tma == 1 else 0.0, 1.0 if p.arith == _lib.UHS_ARITH_DF32 else 0.0,
+                   math.log2(p.tile_z) / 10.0 if p.tile_z > 0 else 0.0, 1.0 if p.kernel == GENERIC else 0.0]
+
+
+N_FEATURES = 8 + 11
+
+
+def features(st: Stencil, p: RunParams) -> list:
+    return class_features(st) + config_features(p)
+
+
+def candidates(st: Stencil) -> list:
+    """Distinct planned launches to try for st (planned without the tuner
+    database so each candidate is what it says)."""
+    out, seen = [], set()
+    ariths = [_lib.UHS_ARITH_DF32, _lib.UHS_ARITH_FMA] if st.dtype == _lib.UHS_F64 else \
+        ([_lib.UHS_ARITH_DF32] if st.dtype == _lib.UHS_F32X2 else [_lib.UHS_ARITH_FMA])
+    tiles = [dict(tile_x=t[0], tile_y=t[1], vy=t[2]) for t in TILES3] if st.rank == 3 else \
+        [dict(tile_x=t) for t in TILES2]
+    zs = [0, 16, 64] if st.rank == 3 else [0, 128, 512]
+    raw = [RunParams(kernel=STREAM, arith=ar, use_tma=tma, tile_z=tz, flags=_lib.UHS_FLAG_NO_TUNE_DB, **t)
+           for ar in ariths for t in tiles for tma in (1, -1) for tz in zs]
+    if st.dtype != _lib.UHS_F32X2:
+        raw.append(RunParams(kernel=GENERIC, arith=_lib.UHS_ARITH_FMA, flags=_lib.UHS_FLAG_NO_TUNE_DB))
+    # plan against the program's contiguous layout (a 256-byte aligned base,
+    # as device allocations are) so loader eligibility is the grid's own
+    layout = memref_raw(1 << 20, st.sizes)
+    for p in raw:
+        try:
+            q = plan(st, layout, params=p)
+        except _lib.UhsError:
+            continue
+        q.flags = _lib.UHS_FLAG_NO_TUNE_DB
+        q.tile_z = p.tile_z
+        key = tuple(asdict(q).values())
+        if key in seen:
+            continue
+        seen.add(key)
+        out.append(q)
+    return out
+
+
+def measure(st: Stencil, a, b, p: RunParams, reps: int = 3, stream=None, min_ms: float = 2.0) -> float:
+    """Nanoseconds per point-update of one sweep with launch p: CUDA events
+    around at least `reps` sweeps (alternating direction) and at least min_ms
+    of GPU time, after one timed warm-up sweep that sizes the count."""
+    import torch
+    q = RunParams(**{**asdict(p), "flags": _lib.UHS_FLAG_NO_SYNC | _lib.UHS_FLAG_NO_TUNE_DB})
+    s1 = st.with_(iterations=1)
+    d = s1.to_desc()
+    ma, mb = memref_of(a), memref_of(b)
+    c = q.to_c()
+    L = _lib.lib()
+    stream = stream or torch.cuda.current_stream()
+    h = stream.cuda_stream
+
+    def timed(k: int) -> float:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(k):
+            src, dst = (ma, mb) if i % 2 == 0 else (mb, ma)
+            _lib.check(L.uhs_sweep(d.ref(), ctypes.byref(src), ctypes.byref(dst), ctypes.byref(c), h))
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    first = max(timed(1), 1e-3)
+    k = int(min(400, max(reps, math.ceil(min_ms / first))))
+    return timed(k) * 1e6 / k / max(1, st.interior_points)
+
+
+def device_grids(st: Stencil, seed: int = 0):
+    """Two device grids for st filled with U[-1,1) (timing inputs)."""
+    import torch
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    shape = st.sizes if st.rank == 3 else st.sizes[1:]
+    a = torch.rand(shape, generator=g, device="cuda", dtype=torch.float64).mul_(2).sub_(1)
+    if st.dtype == _lib.UHS_F32:
+        a = a.float()
+    elif st.dtype == _lib.UHS_F32X2:
+        hi = a.float()
+        lo = (a - hi.double()).float()
+        a = torch.stack([hi, lo], -1).view(torch.float64).reshape(shape)
+    return a, a.clone()
+
+
+class Tuner:
+    """Exhaustive tuner with a JSON database of winners and timing records."""
+
+    def __init__(self, path: str | None = None):
+        self.path = path
+        self.best = {}     # key -> {"params": {...}, "gst": x}
+        self.records = []  # {"features": [...], "ns_per_point": x, "key": ..., "params": {...}}
+        if path and os.path.exists(path):
+            self.load(path)
+
+    @staticmethod
+    def key(st: Stencil) -> str:
+        ext = "x".join(str(u - l) for l, u in zip(st.lb, st.ub))
+        f = class_features(st)
+        return f"r{st.rank}_R{round(f[1] * 3)}_{'box' if f[2] else 'star'}_{st.dtype}_{ext}"
+
+    def tune(self, st: Stencil, a=None, b=None, reps: int = 3, push: bool = True) -> tuple:
+        if a is None:
+            a, b = device_grids(st)
+        results = []
+        for p in candidates(st):
+            try:
+                ns = measure(st, a, b, p, reps)
+            except _lib.UhsError:
+                continue
+            results.append((ns, p))
+            self.records.append({"key": self.key(st), "features": features(st, p), "ns_per_point": ns,
+                                 "params": asdict(p)})
+        if not results:
+            raise RuntimeError(f"no candidate ran for {st.name}")
+        ns, bestp = min(results, key=lambda r: r[0])
+        self.best[self.key(st)] = {"params": asdict(bestp), "gst": 1.0 / ns}
+        if push:
+            push_params(st, bestp, 1.0 / ns)
+        return bestp, results
+
+    def save(self, path: str | None = None) -> None:
+        with open(path or self.path, "w") as f:
+            json.dump({"best": self.best, "records": self.records}, f)
+
+    def load(self, path: str) -> None:
+        with open(path) as f:
+            d = json.load(f)
+        self.best = d.get("best", {})
+        self.records = d.get("records", [])
+
+
+def push_params(st: Stencil, p: RunParams, gst: float) -> None:
+    q = RunParams(**{**asdict(p), "flags": 0})
+    _lib.check(_lib.lib().uhs_tune_put(st.to_desc().ref(), ctypes.byref(q.to_c()), gst))
+
+
+def db_get(st: Stencil):
+    out = _lib.Params()
+    exact = ctypes.c_int32()
+    rc = _lib.lib().uhs_tune_get(st.to_desc().ref(), ctypes.byref(out), ctypes.byref(exact))
+    if rc != _lib.UHS_OK:
+        return None, False
+    return RunParams.from_c(out), bool(exact.value)
+
+
+def db_clear() -> None:
+    _lib.lib().uhs_tune_clear()
