@@ -124,12 +124,14 @@ typedef struct uhs_params {
     int32_t flags;        /* UHS_FLAG_* */
     int32_t vy;           /* points per thread along y (streaming kernel, rank 3) */
     int32_t prefetch;     /* planes loaded ahead of the plane being computed */
-    int32_t reserved[2];
+    int32_t factored;     /* set by uhs_plan: 1 when a separable box runs as 1D passes */
+    int32_t reserved;
 } uhs_params;
 
 enum {
     UHS_FLAG_NO_SYNC = 1,    /* return without synchronising the stream */
-    UHS_FLAG_NO_TUNE_DB = 2  /* ignore the tuner database for this call */
+    UHS_FLAG_NO_TUNE_DB = 2, /* ignore the tuner database for this call */
+    UHS_FLAG_NO_FACTOR = 4   /* sweep a separable box term by term, not as 1D passes */
 };
 
 /* ---- entry points ------------------------------------------------------ */

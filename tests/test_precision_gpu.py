@@ -5,7 +5,7 @@ arithmetic; every 20 steps each is scored on the GPU (uhs_error_norms)
 against the FP64 oracle's state.
 
 Default size is 96^3, T = 200 (the suite's bars: FP64 paths and float pairs
-within 1e-12 of the oracle, FP32 within a relative L2 of 1e-5).  The full
+within 1e-12 of the oracle, FP32 within a relative L2 of 1e-6).  The full
 configuration (512^3, T = 200) runs with UHS_PRECISION_N=512; the table is
 written to UHS_PRECISION_OUT when that is set.
 """
@@ -68,4 +68,4 @@ def test_precision_study(cuda):
     for row in rows:
         for k in ("f32x2", "f64_df32", "f64_native"):
             assert row[k]["max_rel"] <= 1e-12, (row["step"], k, row[k])
-        assert row["f32"]["l2_rel"] <= 1e-5, (row["step"], row["f32"])
+        assert row["f32"]["l2_rel"] <= 1e-6, (row["step"], row["f32"])

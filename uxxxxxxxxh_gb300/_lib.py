@@ -24,7 +24,7 @@ UHS_ARITH_AUTO, UHS_ARITH_FMA, UHS_ARITH_EXACT, UHS_ARITH_DF32 = 0, 1, 2, 3
 # kernel families
 UHS_KERNEL_AUTO, UHS_KERNEL_GENERIC, UHS_KERNEL_STREAM, UHS_KERNEL_MMA = 0, 1, 2, 3
 # flags
-UHS_FLAG_NO_SYNC, UHS_FLAG_NO_TUNE_DB = 1, 2
+UHS_FLAG_NO_SYNC, UHS_FLAG_NO_TUNE_DB, UHS_FLAG_NO_FACTOR = 1, 2, 4
 
 UHS_MAX_TERMS = 512
 UHS_NOALLOC_MAX_PARTIALS = 8192
@@ -55,7 +55,7 @@ class StencilDesc(ctypes.Structure):
 class Params(ctypes.Structure):
     _fields_ = [("kernel", c_int32), ("arith", c_int32), ("tile_x", c_int32), ("tile_y", c_int32),
                 ("tile_z", c_int32), ("k_temporal", c_int32), ("use_tma", c_int32), ("flags", c_int32),
-                ("vy", c_int32), ("prefetch", c_int32), ("reserved", c_int32 * 2)]
+                ("vy", c_int32), ("prefetch", c_int32), ("factored", c_int32), ("reserved", c_int32)]
 
 
 # Every symbol include/*.h declares, with its ctypes signature: (restype, argtypes).

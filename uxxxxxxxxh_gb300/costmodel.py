@@ -2,8 +2,8 @@
 and the launch's features, so the tuner can rank candidates of a program it
 has never timed.
 
-The network is the library's MLP (include/uhs.h, uhs_mlp_*): 19 features ->
-3 x 64 (ReLU) -> 1, trained on the GPU by the library's own forward, backward
+The network is the library's MLP (include/uhs.h, uhs_mlp_*): 23 features
+(tuner.features) -> 3 x 64 (ReLU) -> 1, trained on the GPU by the library's own forward, backward
 and Adam kernels on the tuner's timing records (tuner.Tuner.records).  Target:
 log(ns per point), standardised.  pick() runs the network over every
 candidate of a program and returns the one it predicts fastest; exhaustive
@@ -21,7 +21,7 @@ import numpy as np
 from . import _lib
 from .runtime import RunParams
 from .stencil import Stencil
-from .tuner import N_FEATURES, candidates, features
+from .tuner import N_FEATURES, candidates, class_features, features, measure
 
 
 def _fptr(a: np.ndarray):
@@ -100,10 +100,22 @@ class CostModel:
         y = self.net.forward(np.asarray(feats, np.float32))
         return np.exp(y.astype(np.float64) * self.sigma + self.mu)
 
-    def pick(self, st: Stencil) -> RunParams:
+    def rank(self, st: Stencil) -> list:
+        """Candidates of st ordered by predicted time, fastest first."""
         cands = candidates(st)
-        ns = self.predict_ns([features(st, p) for p in cands])
-        return cands[int(np.argmin(ns))]
+        cls = class_features(st)
+        ns = self.predict_ns([features(st, p, cls) for p in cands])
+        return [cands[i] for i in np.argsort(ns)]
+
+    def pick(self, st: Stencil) -> RunParams:
+        """The candidate the network predicts fastest (no timing)."""
+        return self.rank(st)[0]
+
+    def pick_verified(self, st: Stencil, a, b, k: int = 3, reps: int = 3) -> RunParams:
+        """Time only the network's k best candidates and keep the fastest:
+        k timings instead of the exhaustive search's dozens."""
+        top = self.rank(st)[:k]
+        return min(top, key=lambda p: measure(st, a, b, p, reps))
 
     def save(self, path: str) -> None:
         with open(path, "w") as f:

@@ -20,7 +20,7 @@ namespace {
 // (VY 2, PD 2), rank 2 rows of 256.
 template <int SHAPE, int R, int ST, int AR>
 using BV = std::conditional_t<
-    (SHAPE == kStar2 || SHAPE == kBox2), StreamCfg<SHAPE, R, ST, AR, kLdCpAsync, 256, 1, 1, 4>,
+    is_rank2_shape(SHAPE), StreamCfg<SHAPE, R, ST, AR, kLdCpAsync, 256, 1, 1, 4>,
     std::conditional_t<(SHAPE == kBox3 && R >= 2), StreamCfg<SHAPE, R, ST, AR, kLdCpAsync, 32, 8, 2, 2>,
                        StreamCfg<SHAPE, R, ST, AR, kLdCpAsync, 32, 8, 4, 3>>>;
 
@@ -124,7 +124,7 @@ int batch_kind(int pack, int shape, int R, int st, int ar) {
 }
 
 void batch_tile(int shape, int R, int *bx, int *by, int *zchunk) {
-    if (shape == kStar2 || shape == kBox2) {
+    if (is_rank2_shape(shape)) {
         *bx = 256;
         *by = 1;
         *zchunk = 128;
@@ -171,13 +171,7 @@ void batch_fill_args(BatchArgs *a, const StreamCall &c, int nt) {
     a->shift = 0;
     a->pair_loads = c.pair_loads;
     a->err = c.err;
-    for (int k = 0; k < nt && k < kBatchNT; ++k) {
-        const double v = c.coef[k];
-        const float h = static_cast<float>(v);
-        a->cd[k] = v;
-        a->ch[k] = h;
-        a->cl[k] = static_cast<float>(v - static_cast<double>(h));
-    }
+    fill_coefs(a->cd, a->ch, a->cl, a->cl_sum, c.coef, nt < kBatchNT ? nt : kBatchNT, c.shape, c.R);
 }
 
 }  // namespace uhs

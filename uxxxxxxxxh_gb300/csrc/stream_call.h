@@ -8,7 +8,11 @@
 
 namespace uhs {
 
-enum { kStar3 = 0, kBox3 = 1, kStar2 = 2, kBox2 = 3 };
+enum { kStar3 = 0, kBox3 = 1, kStar2 = 2, kBox2 = 3, kSep3 = 4, kSep2 = 5 };
+// kSep3 / kSep2: box stencils whose coefficients factor as a (x) b (x) c
+// (rank 1), applied as three (two) 1D passes; coefficients [a | b | c].
+// Rank-2 shapes (streamed along y in the kernel frame):
+constexpr bool is_rank2_shape(int shape) { return shape == kStar2 || shape == kBox2 || shape == kSep2; }
 enum { kStF64 = 0, kStF32 = 1, kStF32x2 = 2 };
 enum { kArNative = 0, kArDf32 = 1 };
 enum { kLdCpAsync = 0, kLdTma = 1 };
@@ -31,7 +35,28 @@ struct StreamArgs {
     unsigned *err;
     double cd[NT];
     float ch[NT], cl[NT];
+    // Float grids: sum of the coefficients' float rounding errors (c - ch),
+    // per pass (sep: z, y, x; otherwise [0]); applied once per point to the
+    // centre value so the sweep keeps the FP64 coefficients' sum.
+    float cl_sum[3];
 };
+
+// Coefficients in the three forms the kernels use, plus the per-pass sums of
+// the float rounding errors (separable shapes: passes z | y | x, D each).
+inline void fill_coefs(double *cd, float *ch, float *cl, float *cl_sum, const double *coef, int nt, int shape, int R) {
+    const int D = 2 * R + 1;
+    double sums[3] = {0.0, 0.0, 0.0};
+    for (int k = 0; k < nt; ++k) {
+        const double v = coef[k];
+        const float h = static_cast<float>(v);
+        cd[k] = v;
+        ch[k] = h;
+        cl[k] = static_cast<float>(v - static_cast<double>(h));
+        const int pass = (shape == kSep3 || shape == kSep2) ? k / D : 0;
+        sums[pass < 3 ? pass : 2] += v - static_cast<double>(h);
+    }
+    for (int i = 0; i < 3; ++i) cl_sum[i] = static_cast<float>(sums[i]);
+}
 
 // Everything one streaming launch needs (filled by the runtime).
 struct StreamCall {
@@ -76,7 +101,7 @@ cudaError_t launch_stream_f32x2_2d(const StreamCall &c);
 
 // Geometry of a variant as the kernel template computes it (host mirror).
 inline void stream_box(const StreamCall &c, int eb, int *W, int *H) {
-    const bool is2d = c.shape == kStar2 || c.shape == kBox2;
+    const bool is2d = is_rank2_shape(c.shape);
     const TileShape t = tile_shape(is2d, c.tile);
     const int q = 16 / eb;
     const bool big_box = (c.shape == kBox3 && c.R >= 2);
@@ -85,7 +110,7 @@ inline void stream_box(const StreamCall &c, int eb, int *W, int *H) {
     *H = by + (is2d ? 0 : 2 * c.R);
 }
 inline void stream_tile_xy(const StreamCall &c, int *bx, int *by) {
-    const bool is2d = c.shape == kStar2 || c.shape == kBox2;
+    const bool is2d = is_rank2_shape(c.shape);
     const TileShape t = tile_shape(is2d, c.tile);
     const bool big_box = (c.shape == kBox3 && c.R >= 2);
     *bx = big_box ? 32 : t.bx;
@@ -121,6 +146,12 @@ void batch_tile(int shape, int R, int *bx, int *by, int *zchunk);
 cudaError_t batch_prepare(int pack, BatchPackInfo *info);
 cudaError_t batch_launch(int pack, const BatchGrid *grids, const int4 *items, int n_items, int dir, int ctas,
                          cudaStream_t st);
+// Temporal fusion (stream_fused.cu): K in {2, 4} steps of the 3D 7-point
+// star per pass; and the halo comparison that gates it.
+cudaError_t launch_fused(const StreamCall &c, int K);
+cudaError_t launch_halo_diff(const GridView &a, const GridView &b, int eb, const int64_t lb[3], const int64_t ub[3],
+                             unsigned *count, int sms, cudaStream_t st);
+
 // Host-side packing of one direction's arguments (coefficients in slot order).
 void batch_fill_args(BatchArgs *a, const StreamCall &c, int nt);
 

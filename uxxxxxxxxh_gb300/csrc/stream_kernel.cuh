@@ -38,11 +38,13 @@ namespace uhs {
 
 template <int SHAPE, int R>
 struct ShapeInfo {
-    static constexpr bool is2d = SHAPE >= 2;
+    static constexpr bool is2d = is_rank2_shape(SHAPE);
     static constexpr bool star = (SHAPE == kStar3 || SHAPE == kStar2);
+    static constexpr bool sep = (SHAPE == kSep3 || SHAPE == kSep2);
     static constexpr int RY = is2d ? 0 : R;
     static constexpr int D = 2 * R + 1;
-    static constexpr int NT = star ? (is2d ? 4 * R + 1 : 6 * R + 1) : (is2d ? D * D : D * D * D);
+    static constexpr int NT = sep ? (is2d ? 2 * D : 3 * D)
+                                  : star ? (is2d ? 4 * R + 1 : 6 * R + 1) : (is2d ? D * D : D * D * D);
 };
 
 // Coefficient slot of each offset (the host writes the descriptor's
@@ -85,7 +87,7 @@ struct StreamCfg {
     static constexpr int BY = TYT * VY;
     static constexpr int W = ct_round_up(BX + 2 * R + (LD == kLdTma ? Q - 1 : 0), Q);
     static constexpr int H = BY + 2 * RY;
-    static constexpr int NCMP = SI::star ? R + 1 : 2 * R + 1;
+    static constexpr int NCMP = SI::sep ? 1 : SI::star ? R + 1 : 2 * R + 1;
     static constexpr int NSTG = CONVERT ? PD + 1 : NCMP + PD;
     static constexpr int STG_SLOT = ct_round_up(W * H * EB, 128);
     static constexpr int CMP_SLOT = ct_round_up(W * H * (int)sizeof(TC), 128);
@@ -121,10 +123,12 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
     const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(bar));
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(a), "r"(bytes) : "memory");
 }
-// Bounded wait for phase `parity` of an mbarrier: false when the bound ran out.
+// Bounded wait for phase `parity` of an mbarrier: false when about one second
+// of SM clock (2^31 cycles) passed without the phase completing.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
     const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(bar));
-    for (int i = 0; i < (1 << 22); ++i) {
+    const long long t0 = clock64();
+    for (;;) {
         unsigned done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -132,8 +136,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
+        if (clock64() - t0 > (1ll << 31)) return false;
     }
-    return false;
 }
 __device__ __forceinline__ void tma_load_3d(void *smem, const CUtensorMap *map, int x, int y, int z, uint64_t *bar) {
     const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
@@ -176,13 +180,21 @@ __device__ __forceinline__ float coef_f(const Args &a, const float *p) {
 template <class C, int AR = C::AR>
 struct Arith;
 
+// Native arithmetic: one DFMA / FFMA per term.  Float grids use the float
+// rounding ch of each coefficient; the rounding errors cl = c - ch would sum,
+// for a normalised stencil, to a delta that scales the field by (1 + delta)
+// every step -- an error growing linearly with T.  centre() adds
+// (sum of cl) * centre value once per point, which restores the FP64
+// coefficients' sum exactly (and their action exactly on locally constant
+// fields) for one FFMA.
 template <class C>
 struct Arith<C, kArNative> {
     using TS = typename C::TS;
+    static constexpr bool F32 = std::is_same_v<TS, float>;
     using Acc = TS;
     template <class Args>
     __device__ static __forceinline__ TS coef(const Args &a, int k) {
-        if constexpr (std::is_same_v<TS, double>) return coef_d<C>(a, k);
+        if constexpr (!F32) return coef_d<C>(a, k);
         else return coef_f<C>(a, &a.ch[k]);
     }
     template <class Args>
@@ -193,7 +205,12 @@ struct Arith<C, kArNative> {
     __device__ static __forceinline__ void add(Acc &acc, const Args &a, int k, TS v) {
         acc = fma(coef(a, k), v, acc);
     }
+    template <class Args>
+    __device__ static __forceinline__ void centre(Acc &acc, const Args &a, int pass, TS v) {
+        if constexpr (F32) acc = fmaf(a.cl_sum[pass], v, acc);
+    }
     __device__ static __forceinline__ void store(TS *p, const Acc &acc) { *p = acc; }
+    __device__ static __forceinline__ TS level(const Acc &acc) { return acc; }
 };
 
 template <class C>
@@ -211,6 +228,9 @@ struct Arith<C, kArDf32> {
         if constexpr (C::ST == kStF64) *p = join_f64(acc.h, acc.l);
         else *p = renorm(acc);
     }
+    __device__ static __forceinline__ float2 level(const Acc &acc) { return renorm(acc); }
+    template <class Args>
+    __device__ static __forceinline__ void centre(Acc &, const Args &, int, float2) {}
 };
 
 // ---- the kernel ---------------------------------------------------------
@@ -311,7 +331,8 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
 
     const int cx = tx + R + a.shift;  // smem column of this thread's x
     const int own = (ty * VY + RY) * W + cx;
-    TC q[VY][STAR ? 2 * R + 1 : 1];  // star: z-queue, q[v][R + dz]
+    constexpr bool SEP = C::SI::sep;
+    TC q[VY][(STAR || SEP) ? 2 * R + 1 : 1];  // z-queue, q[v][R + dz]: star: raw values; sep: xy-filtered
     unsigned range_err = 0;
     const bool x_ok = x0 + tx < a.ub2;
     // output pointer of (zs, y0 + ty*VY, x0 + tx); rows beyond ub1 are masked
@@ -334,6 +355,14 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
             if (__syncthreads_or(!ok)) {
                 if (tid == 0) {
                     atomicOr(a.err, kDevErrTimeout);
+                    // first timeout records where it happened: block, plane, slot, phase
+                    if (atomicCAS(a.err + 2, 0u, 1u) == 0u) {
+                        a.err[3] = blockIdx.x;
+                        a.err[4] = blockIdx.z;
+                        a.err[5] = static_cast<unsigned>(j);
+                        a.err[6] = static_cast<unsigned>(s_stg);
+                        a.err[7] = phase;
+                    }
                     for (int k = j; k < min(j + PD, nq); ++k)
                         (void)mbar_wait(mbar + (k % NSTG), static_cast<unsigned>((k / NSTG) & 1));
                 }
@@ -361,6 +390,40 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
         }
         const int slot_j = C::CONVERT ? s_cmp : s_stg;
         const TC *cur = cmp_base + slot_j * CMP_STRIDE;
+        if constexpr (SEP) {
+            // xy-filter the arriving plane for this thread's points and push
+            // the results into the z-queue: x pass per row (rows of the point
+            // column plus the y halo), then y pass (rank 3 only).
+            constexpr int D = 2 * R + 1;
+            constexpr int CX0 = IS2D ? D : 2 * D;  // slot of c (x coefficients)
+            constexpr int NROW = IS2D ? 1 : VY + 2 * R;
+            TC xr[NROW];
+#pragma unroll
+            for (int i = 0; i < NROW; ++i) {
+                const TC *row = cur + own + (IS2D ? 0 : (i - R) * W);
+                Acc t;
+                A::first(t, a, CX0, row[-R]);
+#pragma unroll
+                for (int dx = -R + 1; dx <= R; ++dx) A::add(t, a, CX0 + dx + R, row[dx]);
+                A::centre(t, a, IS2D ? 1 : 2, row[0]);
+                xr[i] = A::level(t);
+            }
+#pragma unroll
+            for (int v = 0; v < VY; ++v) {
+#pragma unroll
+                for (int k = 0; k < 2 * R; ++k) q[v][k] = q[v][k + 1];
+                if constexpr (IS2D) {
+                    q[v][2 * R] = xr[0];
+                } else {
+                    Acc t;
+                    A::first(t, a, D, xr[v]);
+#pragma unroll
+                    for (int dy = -R + 1; dy <= R; ++dy) A::add(t, a, D + dy + R, xr[v + R + dy]);
+                    A::centre(t, a, 1, xr[v + R]);
+                    q[v][2 * R] = A::level(t);
+                }
+            }
+        }
         if constexpr (STAR) {
 #pragma unroll
             for (int v = 0; v < VY; ++v) {
@@ -371,11 +434,22 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
         }
         if (j >= 2 * R) {
             Acc acc[VY];
-            if constexpr (STAR) {
+            if constexpr (SEP) {
+#pragma unroll
+                for (int v = 0; v < VY; ++v) {
+                    A::first(acc[v], a, 0, q[v][0]);
+#pragma unroll
+                    for (int dz = 1; dz < 2 * R + 1; ++dz) A::add(acc[v], a, dz, q[v][dz]);
+                    A::centre(acc[v], a, 0, q[v][R]);
+                }
+            } else if constexpr (STAR) {
                 const int sl = slot_j >= R ? slot_j - R : slot_j - R + NRING;
                 const TC *pl = cmp_base + sl * CMP_STRIDE;
 #pragma unroll
-                for (int v = 0; v < VY; ++v) A::first(acc[v], a, coef_slot<C::SHAPE, R>(0, 0, 0), q[v][R]);
+                for (int v = 0; v < VY; ++v) {
+                    A::first(acc[v], a, coef_slot<C::SHAPE, R>(0, 0, 0), q[v][R]);
+                    A::centre(acc[v], a, 0, q[v][R]);
+                }
 #pragma unroll
                 for (int d = 1; d <= R; ++d)
 #pragma unroll
@@ -415,6 +489,7 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                             const TC v0 = pl[own + dx];
                             if (dz == -R && dx == -R) A::first(acc[0], a, coef_slot<C::SHAPE, R>(dz, 0, dx), v0);
                             else A::add(acc[0], a, coef_slot<C::SHAPE, R>(dz, 0, dx), v0);
+                            if (dz == 0 && dx == 0) A::centre(acc[0], a, 0, v0);
                         }
                     } else {
 #pragma unroll
@@ -430,6 +505,7 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                                         A::first(acc[v], a, coef_slot<C::SHAPE, R>(dz, dy, dx), col[v + R + dy]);
                                     else
                                         A::add(acc[v], a, coef_slot<C::SHAPE, R>(dz, dy, dx), col[v + R + dy]);
+                                    if (dz == 0 && dx == 0 && dy == 0) A::centre(acc[v], a, 0, col[v + R]);
                                 }
                         }
                     }

@@ -33,13 +33,7 @@ cudaError_t launch_cfg(const StreamCall &c) {
     a.shift = c.shift;
     a.pair_loads = c.pair_loads;
     a.err = c.err;
-    for (int k = 0; k < C::NT; ++k) {
-        const double v = c.coef[k];
-        const float h = static_cast<float>(v);
-        a.cd[k] = v;
-        a.ch[k] = h;
-        a.cl[k] = static_cast<float>(v - static_cast<double>(h));
-    }
+    fill_coefs(a.cd, a.ch, a.cl, a.cl_sum, c.coef, C::NT, c.shape, c.R);
     const int64_t nz = c.ub[0] - c.lb[0], ny = c.ub[1] - c.lb[1], nx = c.ub[2] - c.lb[2];
     if (!c.occ_out && (nz <= 0 || ny <= 0 || nx <= 0)) return cudaSuccess;
     static bool attr_set = false;
@@ -93,12 +87,18 @@ cudaError_t dispatch_loader(const StreamCall &c) {
 
 template <int ST, int AR, bool IS2D>
 cudaError_t dispatch_shape(const StreamCall &c) {
-    constexpr int STAR = IS2D ? kStar2 : kStar3, BOX = IS2D ? kBox2 : kBox3;
-    const bool star = (c.shape == kStar2 || c.shape == kStar3);
-    switch (c.R) {
-        case 1: return star ? dispatch_loader<STAR, 1, ST, AR>(c) : dispatch_loader<BOX, 1, ST, AR>(c);
-        case 2: return star ? dispatch_loader<STAR, 2, ST, AR>(c) : dispatch_loader<BOX, 2, ST, AR>(c);
-        case 3: return star ? dispatch_loader<STAR, 3, ST, AR>(c) : dispatch_loader<BOX, 3, ST, AR>(c);
+    constexpr int STAR = IS2D ? kStar2 : kStar3, BOX = IS2D ? kBox2 : kBox3, SEP = IS2D ? kSep2 : kSep3;
+    const int fam = (c.shape == kStar2 || c.shape == kStar3) ? 0 : (c.shape == kSep2 || c.shape == kSep3) ? 2 : 1;
+    switch (c.R * 3 + fam) {
+        case 3: return dispatch_loader<STAR, 1, ST, AR>(c);
+        case 4: return dispatch_loader<BOX, 1, ST, AR>(c);
+        case 5: return dispatch_loader<SEP, 1, ST, AR>(c);
+        case 6: return dispatch_loader<STAR, 2, ST, AR>(c);
+        case 7: return dispatch_loader<BOX, 2, ST, AR>(c);
+        case 8: return dispatch_loader<SEP, 2, ST, AR>(c);
+        case 9: return dispatch_loader<STAR, 3, ST, AR>(c);
+        case 10: return dispatch_loader<BOX, 3, ST, AR>(c);
+        case 11: return dispatch_loader<SEP, 3, ST, AR>(c);
         default: return cudaErrorInvalidValue;
     }
 }

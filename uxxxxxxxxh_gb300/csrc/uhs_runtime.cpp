@@ -57,9 +57,11 @@ unsigned *device_error_word(int device) {
     std::lock_guard<std::mutex> lk(mu);
     if (!words[device]) {
         void *p = nullptr;
-        // word 0: kernel status flags; word 1: range-scan result
-        if (cudaMalloc(&p, 2 * sizeof(unsigned)) != cudaSuccess) return nullptr;
-        cudaMemset(p, 0, 2 * sizeof(unsigned));
+        // word 0: kernel status flags; word 1: range-scan / halo-check result;
+        // words 2-7: where the first bounded wait gave up (set, block x, block z,
+        // plane, ring slot, phase)
+        if (cudaMalloc(&p, 8 * sizeof(unsigned)) != cudaSuccess) return nullptr;
+        cudaMemset(p, 0, 8 * sizeof(unsigned));
         words[device] = static_cast<unsigned *>(p);
     }
     return words[device];
@@ -182,6 +184,7 @@ struct Plan {
     int shape = -1, R = 0, st = 0, ar = 0, ld = kLdCpAsync, tile = 0, zchunk = 0;
     std::vector<double> coef;  // coef_slot order
     bool auto_df32 = false;    // df32 chosen by UHS_ARITH_AUTO, subject to range_ok()
+    bool factored = false;     // separable box run as 1D passes
 };
 
 static int device_sms() {
@@ -241,6 +244,45 @@ static bool classify(const SweepSpec &sp, int *shape, int *R) {
     return true;
 }
 
+// Rank-1 factorisation of a box stencil's coefficient tensor, C = a (x) b (x) c
+// (rank 3) or a (x) c (rank 2; a on the streamed axis).  Exact to a few ulp
+// of max |C| or rejected.  Output: [a | b | c] or [a | c].
+static bool factor_box(const SweepSpec &sp, int R, std::vector<double> *out) {
+    const int D = 2 * R + 1;
+    const bool is2d = sp.rank == 2;
+    std::vector<double> C(is2d ? D * D : D * D * D, 0.0);
+    for (int k = 0; k < sp.nterms; ++k) {
+        const int i = (is2d ? sp.dy[k] : sp.dz[k]) + R, j = sp.dy[k] + R, l = sp.dx[k] + R;
+        C[is2d ? i * D + l : (i * D + j) * D + l] += sp.coef[k];
+    }
+    int piv = 0;
+    for (int n = 1; n < (int)C.size(); ++n)
+        if (std::fabs(C[n]) > std::fabs(C[piv])) piv = n;
+    const double m = C[piv];
+    if (m == 0.0) return false;
+    out->clear();
+    if (is2d) {
+        const int i0 = piv / D, l0 = piv % D;
+        for (int i = 0; i < D; ++i) out->push_back(C[i * D + l0]);
+        for (int l = 0; l < D; ++l) out->push_back(C[i0 * D + l] / m);
+        for (int i = 0; i < D; ++i)
+            for (int l = 0; l < D; ++l)
+                if (std::fabs(C[i * D + l] - (*out)[i] * (*out)[D + l]) > 1e-15 * std::fabs(m)) return false;
+    } else {
+        const int i0 = piv / (D * D), j0 = (piv / D) % D, l0 = piv % D;
+        for (int i = 0; i < D; ++i) out->push_back(C[(i * D + j0) * D + l0]);
+        for (int j = 0; j < D; ++j) out->push_back(C[(i0 * D + j) * D + l0] / m);
+        for (int l = 0; l < D; ++l) out->push_back(C[(i0 * D + j0) * D + l] / m);
+        for (int i = 0; i < D; ++i)
+            for (int j = 0; j < D; ++j)
+                for (int l = 0; l < D; ++l)
+                    if (std::fabs(C[(i * D + j) * D + l] - (*out)[i] * (*out)[D + j] * (*out)[2 * D + l]) >
+                        1e-15 * std::fabs(m))
+                        return false;
+    }
+    return true;
+}
+
 static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &view, Plan *pl) {
     uhs_params dflt;
     uhs_params_default(&dflt);
@@ -256,7 +298,8 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
         return set_error(UHS_EINVAL, "unknown arithmetic mode %d", p->arith);
     if (p->kernel < UHS_KERNEL_AUTO || p->kernel > UHS_KERNEL_MMA)
         return set_error(UHS_EINVAL, "unknown kernel family %d", p->kernel);
-    if (cfg.k_temporal != 1) return set_error(UHS_EUNSUPPORTED, "temporal fusion depth %d is not available", cfg.k_temporal);
+    if (cfg.k_temporal != 1 && cfg.k_temporal != 2 && cfg.k_temporal != 4)
+        return set_error(UHS_EUNSUPPORTED, "temporal fusion depth %d: depths 1, 2 and 4 are available", cfg.k_temporal);
 
     int shape = -1, R = 0;
     const bool shaped = classify(sp, &shape, &R);
@@ -285,6 +328,7 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
         return set_error(UHS_EUNSUPPORTED, "the streaming kernel covers star and box stencils of radius 1-3 in "
                                            "FMA or float-pair arithmetic");
     if (kernel == UHS_KERNEL_GENERIC) {
+        if (cfg.k_temporal > 1) return set_error(UHS_EUNSUPPORTED, "the generic kernel sweeps one step per pass");
         if (arith != UHS_ARITH_FMA && arith != UHS_ARITH_EXACT)
             return set_error(UHS_EUNSUPPORTED, "the generic kernel runs FMA or EXACT arithmetic");
         const int tx = cfg.tile_x > 0 ? cfg.tile_x : 32, ty = cfg.tile_y > 0 ? cfg.tile_y : 8;
@@ -294,6 +338,8 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
         cfg.kernel = kernel;
         return UHS_OK;
     }
+    if (cfg.k_temporal > 1 && !(shape == kStar3 && R == 1 && sp.dtype != UHS_F32X2))
+        return set_error(UHS_EUNSUPPORTED, "temporal fusion covers the 3D 7-point star on FP32/FP64 grids");
     pl->kernel = cfg.kernel = UHS_KERNEL_STREAM;
     pl->shape = shape;
     pl->R = R;
@@ -336,6 +382,14 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
     if (cfg.use_tma > 0 && !tma_ok)
         return set_error(UHS_EUNSUPPORTED, "TMA needs 16-byte aligned grids and row/plane strides");
     pl->ld = tma_ok ? kLdTma : kLdCpAsync;
+    // separable boxes run as 1D passes unless the caller opts out
+    std::vector<double> fac;
+    if ((shape == kBox3 || shape == kBox2) && !(p->flags & UHS_FLAG_NO_FACTOR) && factor_box(sp, R, &fac)) {
+        pl->shape = shape = (shape == kBox3) ? kSep3 : kSep2;
+        pl->coef = fac;
+        pl->factored = true;
+        return UHS_OK;
+    }
     // coefficients in slot order
     pl->coef.assign(nterms_of(shape, R), 0.0);
     for (int k = 0; k < sp.nterms; ++k) {
@@ -394,7 +448,7 @@ static bool make_tmap(const GridView &v, int eb, int W, int H, CUtensorMap *m) {
 }
 
 static cudaError_t stream_dispatch(const StreamCall &c) {
-    const bool is2d = c.shape == kStar2 || c.shape == kBox2;
+    const bool is2d = is_rank2_shape(c.shape);
     if (c.st == kStF64 && c.ar == kArNative) return is2d ? launch_stream_f64n_2d(c) : launch_stream_f64n_3d(c);
     if (c.st == kStF64) return is2d ? launch_stream_f64df_2d(c) : launch_stream_f64df_3d(c);
     if (c.st == kStF32) return is2d ? launch_stream_f32_2d(c) : launch_stream_f32_3d(c);
@@ -506,20 +560,106 @@ static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in,
     return UHS_OK;
 }
 
+// Pass depths for T steps with fusion depth k (1, 2 or 4).  Passes alternate
+// a -> b, b -> a, so an even pass count leaves step T in a; the last pass is a
+// single step so b ends holding step T-1, as the reference's ping-pong does.
+static std::vector<int> plan_passes(int T, int k) {
+    std::vector<int> out;
+    if (T <= 0) return out;
+    if (T == 1 || k <= 1) return std::vector<int>(static_cast<size_t>(T), 1);
+    const int rest = T - 1;  // steps before the final single-step pass (odd count of passes)
+    int best_n = -1, b4 = 0, b2 = 0, b1 = 0;
+    for (int n4 = (k >= 4 ? rest / 4 : 0); n4 >= 0; --n4) {
+        for (int n2 = (rest - 4 * n4) / 2; n2 >= 0; --n2) {
+            const int n1 = rest - 4 * n4 - 2 * n2;
+            const int n = n4 + n2 + n1;
+            if (n % 2 == 1 && (best_n < 0 || n < best_n)) {
+                best_n = n;
+                b4 = n4;
+                b2 = n2;
+                b1 = n1;
+            }
+        }
+    }
+    out.insert(out.end(), static_cast<size_t>(b4), 4);
+    out.insert(out.end(), static_cast<size_t>(b2), 2);
+    out.insert(out.end(), static_cast<size_t>(b1), 1);
+    out.push_back(1);
+    return out;
+}
+
+// Device check that both grids hold byte-identical cells outside the domain.
+static int halos_equal(const SweepSpec &sp, const GridView &a, const GridView &b, cudaStream_t st, bool *eq) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    unsigned *w = device_error_word(dev);
+    if (!w) return set_error(UHS_ENOMEM, "device status word allocation failed");
+    unsigned *cnt = w + 1;
+    cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(unsigned), st);
+    const int eb = sp.dtype == UHS_F32 ? 4 : 8;
+    if (e == cudaSuccess) e = launch_halo_diff(a, b, eb, sp.lb, sp.ub, cnt, device_sms(), st);
+    unsigned h = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, cnt, sizeof h, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "halo comparison");
+    *eq = h == 0;
+    return UHS_OK;
+}
+
+static int launch_fused_pass(const SweepSpec &sp, const Plan &pl, const GridView &in, const GridView &out, int K,
+                             cudaStream_t st) {
+    StreamCall c{};
+    c.shape = pl.shape;
+    c.R = pl.R;
+    c.st = pl.st;
+    c.ar = pl.ar;
+    c.coef = pl.coef.data();
+    c.in = in;
+    c.out = out;
+    for (int i = 0; i < 3; ++i) {
+        c.lb[i] = sp.lb[i];
+        c.ub[i] = sp.ub[i];
+    }
+    c.stream = st;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    c.err = device_error_word(dev);
+    const int64_t nz = sp.ub[0] - sp.lb[0];
+    const int64_t tiles = ((sp.ub[2] - sp.lb[2] + 31) / 32) * ((sp.ub[1] - sp.lb[1] + 15) / 16);
+    int zchunk = pl.cfg.tile_z;
+    if (zchunk <= 0 && nz > 0 && tiles > 0) {
+        int occ = 0;
+        StreamCall q = c;
+        q.occ_out = &occ;
+        if (launch_fused(q, K) != cudaSuccess || occ <= 0) occ = 1;
+        const int64_t want = static_cast<int64_t>(device_sms()) * occ * 3;
+        const int64_t chunks = std::max<int64_t>(1, (want + tiles - 1) / tiles);
+        zchunk = static_cast<int>(std::max<int64_t>(8 * K, (nz + chunks - 1) / chunks));
+    }
+    c.zchunk = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(zchunk, std::max<int64_t>(nz, 1))));
+    cudaError_t e = launch_fused(c, K);
+    if (e != cudaSuccess) return cuda_error(e, "fused sweep launch");
+    return UHS_OK;
+}
+
 // Read and clear the device error word after the stream drained.
 static int check_device_errors(cudaStream_t st) {
     int dev = 0;
     cudaGetDevice(&dev);
     unsigned *w = device_error_word(dev);
     if (!w) return UHS_OK;
-    unsigned h = 0;
-    cudaError_t e = cudaMemcpyAsync(&h, w, sizeof h, cudaMemcpyDeviceToHost, st);
+    unsigned h[8] = {};
+    cudaError_t e = cudaMemcpyAsync(h, w, sizeof h, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_error(e, "device status read");
-    if (!h) return UHS_OK;
-    cudaMemsetAsync(w, 0, sizeof(unsigned), st);
+    if (!h[0]) return UHS_OK;
+    cudaMemsetAsync(w, 0, sizeof h, st);
     cudaStreamSynchronize(st);
-    if (h & kDevErrTimeout) return set_error(UHS_ETIMEOUT, "a kernel's bounded wait for its plane loads ran out");
+    if (h[0] & kDevErrTimeout)
+        return set_error(UHS_ETIMEOUT,
+                         "a kernel's bounded wait for its plane loads ran out (block %u,%u, plane %u, slot %u, "
+                         "phase %u)",
+                         h[3], h[4], h[5], h[6], h[7]);
     return set_error(UHS_ERANGE, "a grid value is outside the float-pair range [2^-126, 2^128); "
                                  "run this grid with UHS_ARITH_FMA");
 }
@@ -636,7 +776,11 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
         SweepSpec sp;
         make_spec(&descs[i], &sp);
         Plan pl;
-        if ((rc = plan_sweep(sp, params, va, &pl))) return set_error(rc, "program %d: %s", i, uhs_last_error());
+        uhs_params bp;
+        if (params) bp = *params;
+        else uhs_params_default(&bp);
+        bp.flags |= UHS_FLAG_NO_FACTOR;  // the batched packs sweep boxes term by term
+        if ((rc = plan_sweep(sp, &bp, va, &pl))) return set_error(rc, "program %d: %s", i, uhs_last_error());
         if (pl.kernel != UHS_KERNEL_STREAM)
             return set_error(UHS_EUNSUPPORTED, "program %d is not a star/box stencil the batched kernel covers", i);
         if (pl.auto_df32 && descs[i].iterations > 0 && !range_ok(sp, va, vb, descs[i].iterations, scan_stream)) {
@@ -964,6 +1108,7 @@ int uhs_plan(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_params *p
         out->tile_y = sp.rank == 3 ? by : 1;
         out->vy = sp.rank == 3 ? tile_shape(false, (pl.shape == kBox3 && pl.R >= 2) ? 3 : pl.tile).vy : 1;
         out->use_tma = pl.ld == kLdTma ? 1 : -1;
+        out->factored = pl.factored ? 1 : 0;
     } else {
         out->tile_x = pl.cfg.tile_x > 0 ? pl.cfg.tile_x : 32;
         out->tile_y = pl.cfg.tile_y > 0 ? pl.cfg.tile_y : 8;
@@ -1009,6 +1154,22 @@ int uhs_run(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_memref *b,
     if (pl.auto_df32 && d->iterations > 0 && !range_ok(sp, va, vb, d->iterations, st)) {
         pl.ar = kArNative;
         pl.cfg.arith = UHS_ARITH_FMA;
+    }
+    if (pl.kernel == UHS_KERNEL_STREAM && pl.cfg.k_temporal > 1 && d->iterations > 1) {
+        bool eq = false;
+        if ((rc = halos_equal(sp, va, vb, st, &eq))) return rc;
+        if (!eq)
+            return set_error(UHS_EINVAL, "temporal fusion needs both grids to hold the same values outside the "
+                                         "domain (the halo); run with k_temporal = 1");
+        const std::vector<int> passes = plan_passes(d->iterations, pl.cfg.k_temporal);
+        bool fwd = true;
+        for (int depth : passes) {
+            const GridView &in = fwd ? va : vb, &out = fwd ? vb : va;
+            rc = depth == 1 ? launch_sweep(sp, pl, in, out, st) : launch_fused_pass(sp, pl, in, out, depth, st);
+            if (rc) return rc;
+            fwd = !fwd;
+        }
+        return finish(p, st);
     }
     if (d->iterations == 1) {
         if ((rc = launch_sweep(sp, pl, va, vb, st))) return rc;

@@ -35,18 +35,26 @@ TILES2 = [64, 128, 256]
 
 
 def class_features(st: Stencil) -> list:
-    """Program features: rank, radius, box, FP64, log2 extents, log2 terms."""
+    """Program features: rank, radius, box, FP64, log2 extents, log2 terms,
+    and whether the planner sweeps it as separable 1D passes."""
     rz, ry, rx = st.radius
     r = max(rz, ry, rx)
     box = any(sum(1 for v in t[:3] if v != 0) > 1 for t in st.terms)
     ext = [max(1, u - l) for l, u in zip(st.lb, st.ub)]
+    try:
+        factored = plan(st, memref_raw(1 << 20, st.sizes),
+                        params=RunParams(flags=_lib.UHS_FLAG_NO_TUNE_DB)).factored
+    except _lib.UhsError:
+        factored = 0
     return [1.0 if st.rank == 3 else 0.0, r / 3.0, 1.0 if box else 0.0, 1.0 if st.dtype != _lib.UHS_F32 else 0.0,
             math.log2(ext[0]) / 10.0, math.log2(ext[1]) / 10.0, math.log2(ext[2]) / 13.0,
-            math.log2(len(st.terms)) / 9.0]
+            math.log2(len(st.terms)) / 9.0, float(factored)]
 
 
-def config_features(p: RunParams) -> list:
-    """Launch features of a planned configuration."""
+def config_features(p: RunParams, st: Stencil | None = None) -> list:
+    """Launch features of a planned configuration: tile one-hot, loader,
+    arithmetic, z-chunk, generic kernel, and (given the program) how the tile
+    quantises its domain: log2 CTA tiles and the idle fraction of edge tiles."""
     tile = [0.0] * 7
     if p.kernel == STREAM:
         if p.tile_y > 1:
@@ -55,15 +63,22 @@ def config_features(p: RunParams) -> list:
                 tile[TILES3.index(key)] = 1.0
         elif p.tile_x in TILES2:
             tile[4 + TILES2.index(p.tile_x)] = 1.0
+    quant = [0.0, 0.0, 0.0]
+    if st is not None and p.tile_x > 0:
+        ext = [max(1, u - l) for l, u in zip(st.lb, st.ub)]
+        ty = max(1, p.tile_y)
+        tx_n, ty_n = math.ceil(ext[2] / p.tile_x), math.ceil(ext[1] / ty) if st.rank == 3 else 1
+        quant = [math.log2(tx_n * ty_n) / 16.0, tx_n * p.tile_x / ext[2] - 1.0,
+                 (ty_n * ty / ext[1] - 1.0) if st.rank == 3 else 0.0]
     return tile + [1.0 if p.use_tma == 1 else 0.0, 1.0 if p.arith == _lib.UHS_ARITH_DF32 else 0.0,
-                   math.log2(p.tile_z) / 10.0 if p.tile_z > 0 else 0.0, 1.0 if p.kernel == GENERIC else 0.0]
+                   math.log2(p.tile_z) / 10.0 if p.tile_z > 0 else 0.0, 1.0 if p.kernel == GENERIC else 0.0] + quant
 
 
-N_FEATURES = 8 + 11
+N_FEATURES = 9 + 14
 
 
-def features(st: Stencil, p: RunParams) -> list:
-    return class_features(st) + config_features(p)
+def features(st: Stencil, p: RunParams, cls: list | None = None) -> list:
+    return (cls if cls is not None else class_features(st)) + config_features(p, st)
 
 
 def candidates(st: Stencil) -> list:
@@ -163,13 +178,14 @@ class Tuner:
         if a is None:
             a, b = device_grids(st)
         results = []
+        cls = class_features(st)
         for p in candidates(st):
             try:
                 ns = measure(st, a, b, p, reps)
             except _lib.UhsError:
                 continue
             results.append((ns, p))
-            self.records.append({"key": self.key(st), "features": features(st, p), "ns_per_point": ns,
+            self.records.append({"key": self.key(st), "features": features(st, p, cls), "ns_per_point": ns,
                                  "params": asdict(p)})
         if not results:
             raise RuntimeError(f"no candidate ran for {st.name}")
