@@ -66,6 +66,21 @@ cudaError_t launch_error_norms(const ErrNormsCall &c);
 // *out must start at 0).
 cudaError_t launch_max_exponent(const void *data, int64_t n_words, unsigned *out, int sms, cudaStream_t st);
 
+// FP32 3D box stencils of radius 2 and 3 on the tensor cores (box_mma.cu).
+// Coefficients in box slot order ((dz+R)*D + (dy+R))*D + (dx+R), D = 2R+1.
+// xtile: 16 or 32 output columns per CTA tile (32 for R = 2 only).
+struct MmaCall {
+    GridView in, out;
+    int64_t lb[3], ub[3];
+    int R;
+    int xtile;
+    const double *coef;
+    unsigned *err;
+    cudaStream_t stream;
+    int *occ_out;  // when set: report CTAs per SM and launch nothing
+};
+cudaError_t launch_box_mma(const MmaCall &c);
+
 // Launch counter shared by every launcher.
 void count_launch(int n = 1);
 

@@ -323,7 +323,31 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
     int kernel = p->kernel;
     const bool stream_ok = shaped && arith != UHS_ARITH_EXACT;
     if (kernel == UHS_KERNEL_AUTO) kernel = stream_ok ? UHS_KERNEL_STREAM : UHS_KERNEL_GENERIC;
-    if (kernel == UHS_KERNEL_MMA) return set_error(UHS_EUNSUPPORTED, "the tensor-core box path is not available");
+    if (kernel == UHS_KERNEL_MMA) {
+        // tcgen05 kind::tf32 with split operands: FP32 3D boxes of radius 2 and 3
+        if (!(sp.dtype == UHS_F32 && shaped && shape == kBox3 && (R == 2 || R == 3)))
+            return set_error(UHS_EUNSUPPORTED, "the tensor-core path covers FP32 3D box stencils of radius 2 and 3");
+        if (arith != UHS_ARITH_FMA)
+            return set_error(UHS_EUNSUPPORTED, "the tensor-core path computes in split-tf32 FMA arithmetic");
+        if (cfg.k_temporal > 1) return set_error(UHS_EUNSUPPORTED, "the tensor-core path sweeps one step per pass");
+        int xt = cfg.tile_x > 0 ? cfg.tile_x : (R == 2 ? 32 : 16);
+        if (!(xt == 16 || (xt == 32 && R == 2)))
+            return set_error(UHS_EINVAL, "tensor-core tiles are 16 columns wide (32 for radius 2), got %d", xt);
+        if (view.s[0] >= (int64_t(1) << 31) || view.n[0] >= (int64_t(1) << 31))
+            return set_error(UHS_EUNSUPPORTED, "planes of 2^31 elements or more need the generic kernel");
+        pl->kernel = cfg.kernel = UHS_KERNEL_MMA;
+        cfg.tile_x = xt;
+        cfg.tile_y = 128;
+        cfg.use_tma = -1;
+        pl->shape = shape;
+        pl->R = R;
+        pl->st = kStF32;
+        pl->ar = kArNative;
+        pl->tile = xt;
+        pl->coef.assign(nterms_of(shape, R), 0.0);
+        for (int k = 0; k < sp.nterms; ++k) pl->coef[coef_slot_rt(shape, R, sp.dz[k], sp.dy[k], sp.dx[k])] += sp.coef[k];
+        return UHS_OK;
+    }
     if (kernel == UHS_KERNEL_STREAM && !stream_ok)
         return set_error(UHS_EUNSUPPORTED, "the streaming kernel covers star and box stencils of radius 1-3 in "
                                            "FMA or float-pair arithmetic");
@@ -496,6 +520,26 @@ static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in,
     if (pl.kernel == UHS_KERNEL_GENERIC) {
         cudaError_t e = launch_generic(sp, pl.cfg, in, out, st);
         if (e != cudaSuccess) return cuda_error(e, "generic sweep launch");
+        return UHS_OK;
+    }
+    if (pl.kernel == UHS_KERNEL_MMA) {
+        MmaCall m{};
+        m.in = in;
+        m.out = out;
+        for (int i = 0; i < 3; ++i) {
+            m.lb[i] = sp.lb[i];
+            m.ub[i] = sp.ub[i];
+        }
+        m.R = pl.R;
+        m.xtile = pl.tile;
+        m.coef = pl.coef.data();
+        m.stream = st;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        m.err = device_error_word(dev);
+        if (!m.err) return set_error(UHS_ENOMEM, "device error word allocation failed");
+        cudaError_t e = launch_box_mma(m);
+        if (e != cudaSuccess) return cuda_error(e, "tensor-core box sweep launch");
         return UHS_OK;
     }
     StreamCall c{};

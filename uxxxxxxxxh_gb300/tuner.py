@@ -117,7 +117,7 @@ def measure(st: Stencil, a, b, p: RunParams, reps: int = 3, stream=None, min_ms:
     around at least `reps` sweeps (alternating direction) and at least min_ms
     of GPU time, after one timed warm-up sweep that sizes the count."""
     import torch
-    q = RunParams(**{**asdict(p), "flags": _lib.UHS_FLAG_NO_SYNC | _lib.UHS_FLAG_NO_TUNE_DB})
+    q = RunParams(**{**asdict(p), "flags": p.flags | _lib.UHS_FLAG_NO_SYNC | _lib.UHS_FLAG_NO_TUNE_DB})
     s1 = st.with_(iterations=1)
     d = s1.to_desc()
     ma, mb = memref_of(a), memref_of(b)
