@@ -48,8 +48,9 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg4", "cfg5"])
-    p.add_argument("--n", type=int, default=0, help="interior side override (smaller case for profiling)")
+    p.add_argument("--side", type=int, default=0, help="interior side override (smaller case for profiling)")
     p.add_argument("--iters", type=int, default=0, help="T override")
+    p.add_argument("--dtype", choices=["f64", "f32"], default="f64", help="grid element type of the main run")
     p.add_argument("--arith", type=int, default=0)
     p.add_argument("--kernel", type=int, default=0)
     p.add_argument("--no-cpu", action="store_true", help="skip the oracle (profiling runs)")
@@ -71,11 +72,15 @@ def make_workload(args):
     from uxxxxxxxxh_gb300 import workloads as W
     fn = getattr(W, args.config)
     kw = {}
-    if args.n:
-        kw["n"] = args.n
+    if args.side:
+        kw["n"] = args.side
     if args.iters:
         kw["T"] = args.iters
-    return fn(**kw)
+    st, a0 = fn(**kw)
+    if getattr(args, "dtype", "f64") == "f32":
+        from uxxxxxxxxh_gb300._lib import UHS_F32
+        st = st.with_(dtype=UHS_F32)
+    return st, a0
 
 
 class Clocks:
@@ -166,6 +171,83 @@ def run_reference(args, rank: int, world: int):
             "cpu_baseline": samp,
             "e2e": {"value": v, "unit": "GStencil/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def reduce_max_ms(ms: float, dist, device) -> float:
+    """Max over ranks of each replica's own timing (a no-op on one rank)."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_gst(points_per_step: int, steps: int, ms: float, world: int) -> float:
+    """Whole-job GStencil/s: every rank sweeps its own replica of the
+    workload, so the job processes world * points per step in the max time."""
+    return world * points_per_step * steps / (ms * 1e-3) / 1e9
+
+
+def sweep_launch_ms(uhs, st, a, b, plan, stream, n: int) -> float:
+    """Average duration of the sweep kernel alone: n single-sweep calls with
+    the planned launch (alternating direction), CUDA events on the stream the
+    kernel is launched on."""
+    import torch
+    q = uhs.RunParams(**{**plan.__dict__, "flags": uhs._lib.UHS_FLAG_NO_SYNC | uhs._lib.UHS_FLAG_NO_TUNE_DB})
+    s1 = st.with_(iterations=1)
+    uhs.sweep(s1, a, b, q, stream=stream)
+    uhs.sweep(s1, b, a, q, stream=stream)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(n):
+        src, dst = (a, b) if i % 2 == 0 else (b, a)
+        uhs.sweep(s1, src, dst, q, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / n
+
+
+def box_paths(uhs, args, stream):
+    """The 343-point Gaussian box (cfg3) on every path the backend has for
+    it: FP32 grids on the CUDA cores term by term, as separable 1D passes and
+    on the tensor cores (split-tf32 tcgen05), FP64 grids term by term (float
+    pairs and native FP64) and separable; GStencil/s of one whole run and the
+    error against the FP64 oracle."""
+    import torch
+    import oracle
+    st, a0 = make_workload(args)
+    oracle.set_threads(os.cpu_count() or 1)
+    ra, rb = a0.copy(), a0.copy()
+    oracle.iterate_f64(st, ra, rb)
+    F = uhs._lib
+    paths = {
+        "f32_cuda_cores": (F.UHS_F32, uhs.RunParams(kernel=F.UHS_KERNEL_STREAM, flags=F.UHS_FLAG_NO_FACTOR)),
+        "f32_separable": (F.UHS_F32, uhs.RunParams(kernel=F.UHS_KERNEL_STREAM)),
+        "f32_tensor_cores": (F.UHS_F32, uhs.RunParams(kernel=F.UHS_KERNEL_MMA)),
+        "f64_df32_cuda_cores": (F.UHS_F64, uhs.RunParams(arith=F.UHS_ARITH_DF32, flags=F.UHS_FLAG_NO_FACTOR)),
+        "f64_native_cuda_cores": (F.UHS_F64, uhs.RunParams(arith=F.UHS_ARITH_FMA, flags=F.UHS_FLAG_NO_FACTOR)),
+        "f64_separable": (F.UHS_F64, uhs.RunParams(arith=F.UHS_ARITH_DF32)),
+    }
+    out = {}
+    for name, (dt, p) in paths.items():
+        s = st.with_(dtype=dt)
+        tdt = torch.float32 if dt == F.UHS_F32 else torch.float64
+        a = torch.from_numpy(a0.reshape(st.sizes)).to(tdt).cuda()
+        b = a.clone()
+        q = uhs.RunParams(**{**p.__dict__, "flags": p.flags | F.UHS_FLAG_NO_SYNC})
+        with torch.cuda.stream(stream):
+            ms, _ = timed_runs(uhs, s, a, b, q, max(1, args.steps), max(1, args.warmup), stream)
+        a.copy_(torch.from_numpy(a0.reshape(st.sizes)).to(tdt))
+        b.copy_(a)
+        uhs.run(s, a, b, p)
+        e = oracle.error(st, ra, a.double().cpu().numpy().reshape(-1))
+        out[name] = {"gstencil_s": st.interior_points * st.iterations * max(1, args.steps) / (ms * 1e-3) / 1e9,
+                     "l2_rel": e["l2_rel"], "max_rel": e["max_rel"], "kernel": uhs.plan(s, a, p).kernel}
+        del a, b
+    return out
 
 
 def timed_runs(uhs, st, a, b, params, steps, warmup, stream, dist=None):
@@ -266,7 +348,8 @@ def main():
     st, a0 = make_workload(args)
     params = uhs.RunParams(kernel=args.kernel, arith=args.arith, flags=uhs._lib.UHS_FLAG_NO_SYNC)
     stream = torch.cuda.Stream()
-    dev_a = torch.from_numpy(a0.reshape(st.sizes)).cuda()
+    tdt = torch.float32 if st.dtype == uhs.UHS_F32 else torch.float64
+    dev_a = torch.from_numpy(a0.reshape(st.sizes)).to(tdt).cuda()
     dev_b = dev_a.clone()
     torch.cuda.synchronize()
 
@@ -275,26 +358,25 @@ def main():
     with torch.cuda.stream(stream):
         ms, launches = timed_runs(uhs, st, dev_a, dev_b, params, args.steps, args.warmup, stream, dist)
     clk = clocks.stop()
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = reduce_max_ms(ms, dist, "cuda")
     pts = st.interior_points * st.iterations
-    value = world * pts * args.steps / (ms * 1e-3) / 1e9
+    value = aggregate_gst(pts, args.steps, ms, world)
     ms_step = ms / args.steps
     plan = uhs.plan(st, dev_a, params)
 
-    # Roofline of the sweep kernel: algorithmic bytes per launch / avg launch
-    # time.  A step launches T sweeps (plus, under UHS_ARITH_AUTO on FP64, two
-    # short range scans); the whole step time is charged to the sweeps, so the
-    # achieved bandwidth is a slight underestimate.
+    # Roofline of the dominant kernel (the sweep): algorithmic bytes per
+    # launch (one read and one write of every interior element) over the
+    # kernel's own average duration, timed here on its stream.
     eb = st.elem_bytes
     launches_per_step = max(1, launches // max(1, args.steps))
     sweeps = st.iterations * args.steps
-    avg_launch_s = (ms * 1e-3) / max(1, sweeps)
     alg_bytes = 2 * eb * st.interior_points
     peak, peak_kind = load_peaks()
+    with torch.cuda.stream(stream):
+        kernel_ms = sweep_launch_ms(uhs, st, dev_a, dev_b, plan, stream, n=max(10, min(2 * st.iterations, 40)))
+    avg_launch_s = kernel_ms * 1e-3
     achieved = alg_bytes / avg_launch_s / 1e9
+    step_sweep_ms = ms / max(1, sweeps)
 
     # Correctness of this exact run against the oracle (fresh input).
     errs = None
@@ -303,12 +385,14 @@ def main():
         import oracle
         oracle.set_threads(os.cpu_count() or 1)
         cpu = cpu_sample(st, a0)
-        ra, rb = a0.copy(), a0.copy()
+        # FP32 runs are scored against the oracle on the same (rounded) input
+        src = a0 if st.dtype != uhs.UHS_F32 else a0.astype(np.float32).astype(np.float64)
+        ra, rb = src.copy(), src.copy()
         oracle.iterate_f64(st, ra, rb)
         dev_a.copy_(torch.from_numpy(a0.reshape(st.sizes)))
         dev_b.copy_(dev_a)
         uhs.run(st, dev_a, dev_b, uhs.RunParams(kernel=args.kernel, arith=args.arith))
-        got = dev_a.cpu().numpy().reshape(-1)
+        got = dev_a.double().cpu().numpy().reshape(-1)
         errs = oracle.error(st, ra, got)
         errs["halo_bit_exact"] = oracle.halo_diff(st, ra, got) == 0
 
@@ -335,7 +419,7 @@ def main():
     # End to end through the C ABI with host buffers.
     e2e = None
     if not args.no_e2e:
-        host_in = torch.from_numpy(a0.reshape(st.sizes)).pin_memory()
+        host_in = torch.from_numpy(a0.reshape(st.sizes)).to(tdt).pin_memory()
         host_out = torch.empty_like(host_in).pin_memory()
         with torch.cuda.stream(stream):
             for it in range(args.warmup + args.steps):
@@ -352,18 +436,16 @@ def main():
                 host_out.copy_(dev_a, non_blocking=True)
             f1.record(stream)
             torch.cuda.synchronize()
-        ems = f0.elapsed_time(f1)
-        if dist:
-            t = torch.tensor([ems], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ems = float(t.item())
+        ems = reduce_max_ms(f0.elapsed_time(f1), dist, "cuda")
         nbytes = host_in.numel() * host_in.element_size()
-        e2e = {"value": world * pts * args.steps / (ems * 1e-3) / 1e9, "unit": "GStencil/s",
+        e2e = {"value": aggregate_gst(pts, args.steps, ems, world), "unit": "GStencil/s",
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": ems / args.steps}
 
     if rank != 0:
         return
     name = {0: "f64", 1: "f32"}.get(st.dtype, "f32x2")
+    if plan.kernel == uhs.UHS_KERNEL_MMA:
+        name = "f32 (split-tf32 tensor cores)"
     arith_names = {1: "fma", 2: "exact", 3: "df32"}
     line = {
         "metric": "GStencil/s", "value": value, "unit": "GStencil/s", "n_gpus": world, "steps": args.steps,
@@ -377,7 +459,8 @@ def main():
         "pct_hbm_roofline": achieved / peak,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                     "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_launch_s * 1e3},
+                     "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_launch_s * 1e3,
+                     "step_time_per_sweep_ms": step_sweep_ms},
         "gpu_launches": launches,
         "launches_per_step": launches_per_step,
         "sweep_launches": sweeps,
@@ -387,6 +470,8 @@ def main():
         "error_vs_oracle": errs,
         "fp32": fp32,
     }
+    if args.config == "cfg3" and not args.no_cpu:
+        line["box_paths"] = box_paths(uhs, args, stream)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

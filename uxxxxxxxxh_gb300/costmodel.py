@@ -2,7 +2,7 @@
 and the launch's features, so the tuner can rank candidates of a program it
 has never timed.
 
-The network is the library's MLP (include/uhs.h, uhs_mlp_*): 23 features
+The network is the library's MLP (include/uhs.h, uhs_mlp_*): 24 features
 (tuner.features) -> 3 x 64 (ReLU) -> 1, trained on the GPU by the library's own forward, backward
 and Adam kernels on the tuner's timing records (tuner.Tuner.records).  Target:
 log(ns per point), standardised.  pick() runs the network over every
@@ -15,6 +15,7 @@ from __future__ import annotations
 import ctypes
 import json
 import math
+import os
 
 import numpy as np
 
@@ -22,6 +23,9 @@ from . import _lib
 from .runtime import RunParams
 from .stencil import Stencil
 from .tuner import N_FEATURES, candidates, class_features, features, measure
+
+# The model trained on GB300 timings by tuner_study (shipped with the package).
+DEFAULT_MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "costmodel.json")
 
 
 def _fptr(a: np.ndarray):
@@ -119,13 +123,21 @@ class CostModel:
 
     def save(self, path: str) -> None:
         with open(path, "w") as f:
-            json.dump({"hidden": self.net.hidden, "layers": self.net.layers, "mu": self.mu, "sigma": self.sigma,
+            json.dump({"features": N_FEATURES, "hidden": self.net.hidden, "layers": self.net.layers,
+                       "mu": self.mu, "sigma": self.sigma,
                        "trained_on": self.trained_on, "params": self.net.get_params().tolist()}, f)
+
+    @staticmethod
+    def default() -> "CostModel":
+        """The shipped model (data/costmodel.json)."""
+        return CostModel.load(DEFAULT_MODEL)
 
     @staticmethod
     def load(path: str) -> "CostModel":
         with open(path) as f:
             d = json.load(f)
+        if d.get("features", N_FEATURES) != N_FEATURES:
+            raise ValueError(f"{path}: model of {d.get('features')} features, this library has {N_FEATURES}")
         m = CostModel(d["hidden"], d["layers"])
         m.mu, m.sigma, m.trained_on = d["mu"], d["sigma"], d.get("trained_on", 0)
         m.net.set_params(np.array(d["params"], np.float32))

@@ -14,8 +14,9 @@ record for the learned cost model (costmodel.py).
 Candidates (rank 3): tile {32x32 VY4, 32x16 VY4, 64x8 VY2, 32x16 VY2} x
 loader {TMA, cp.async} x z-chunk {auto, 16, 64} x arithmetic (FP64:
 {float pairs, native}); rank 2: rows {64, 128, 256} x loader x z-chunk
-{auto, 128, 512} x arithmetic; plus the generic kernel.  Candidates that plan
-to the same launch are timed once.
+{auto, 128, 512} x arithmetic; plus the generic kernel, and for FP32 3D boxes
+of radius 2 and 3 the tensor-core kernel (16 or 32 columns).  Candidates that
+plan to the same launch are timed once.
 """
 from __future__ import annotations
 
@@ -29,7 +30,7 @@ from . import _lib
 from .runtime import RunParams, memref_of, memref_raw, plan
 from .stencil import Stencil
 
-STREAM, GENERIC = _lib.UHS_KERNEL_STREAM, _lib.UHS_KERNEL_GENERIC
+STREAM, GENERIC, MMA = _lib.UHS_KERNEL_STREAM, _lib.UHS_KERNEL_GENERIC, _lib.UHS_KERNEL_MMA
 TILES3 = [(32, 32, 4), (32, 16, 4), (64, 8, 2), (32, 16, 2)]
 TILES2 = [64, 128, 256]
 
@@ -71,10 +72,11 @@ def config_features(p: RunParams, st: Stencil | None = None) -> list:
         quant = [math.log2(tx_n * ty_n) / 16.0, tx_n * p.tile_x / ext[2] - 1.0,
                  (ty_n * ty / ext[1] - 1.0) if st.rank == 3 else 0.0]
     return tile + [1.0 if p.use_tma == 1 else 0.0, 1.0 if p.arith == _lib.UHS_ARITH_DF32 else 0.0,
-                   math.log2(p.tile_z) / 10.0 if p.tile_z > 0 else 0.0, 1.0 if p.kernel == GENERIC else 0.0] + quant
+                   math.log2(p.tile_z) / 10.0 if p.tile_z > 0 else 0.0, 1.0 if p.kernel == GENERIC else 0.0,
+                   1.0 if p.kernel == MMA else 0.0] + quant
 
 
-N_FEATURES = 9 + 14
+N_FEATURES = 9 + 15
 
 
 def features(st: Stencil, p: RunParams, cls: list | None = None) -> list:
@@ -94,6 +96,8 @@ def candidates(st: Stencil) -> list:
            for ar in ariths for t in tiles for tma in (1, -1) for tz in zs]
     if st.dtype != _lib.UHS_F32X2:
         raw.append(RunParams(kernel=GENERIC, arith=_lib.UHS_ARITH_FMA, flags=_lib.UHS_FLAG_NO_TUNE_DB))
+    if st.dtype == _lib.UHS_F32 and st.rank == 3:
+        raw += [RunParams(kernel=MMA, tile_x=tx, flags=_lib.UHS_FLAG_NO_TUNE_DB) for tx in (16, 32)]
     # plan against the program's contiguous layout (a 256-byte aligned base,
     # as device allocations are) so loader eligibility is the grid's own
     layout = memref_raw(1 << 20, st.sizes)
