@@ -59,6 +59,14 @@ def parse_args():
     return p.parse_args()
 
 
+# DRAM bytes per point-update of the 7-point star sweep kernels, from one ncu
+# capture of each on GB300 (320^3 interior, dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch over its 32.8 M points).  A launch's
+# traffic grows with the points it sweeps, so the per-launch figure for
+# another size is this times its interior points.
+NCU_BYTES_PER_POINT = {("star7", "f64", "df32"): 15.10, ("star7", "f64", "fma"): 15.20, ("star7", "f32", "fma"): 6.77}
+
+
 def load_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -443,10 +451,13 @@ def main():
 
     if rank != 0:
         return
+    arith_names = {1: "fma", 2: "exact", 3: "df32"}
     name = {0: "f64", 1: "f32"}.get(st.dtype, "f32x2")
+    star7 = st.rank == 3 and len(st.terms) == 7 and max(st.radius) == 1
+    bpp = NCU_BYTES_PER_POINT.get(("star7", name, arith_names.get(plan.arith, "")), None) if star7 else None
+    traffic = bpp * st.interior_points if bpp else None
     if plan.kernel == uhs.UHS_KERNEL_MMA:
         name = "f32 (split-tf32 tensor cores)"
-    arith_names = {1: "fma", 2: "exact", 3: "df32"}
     line = {
         "metric": "GStencil/s", "value": value, "unit": "GStencil/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -458,7 +469,10 @@ def main():
                    "tile": [plan.tile_x, plan.tile_y, plan.tile_z], "k_temporal": plan.k_temporal},
         "pct_hbm_roofline": achieved / peak,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "traffic": traffic,
+                     "traffic_source": "ncu DRAM bytes of one launch of this kernel at 320^3, scaled by points"
+                     if traffic else None,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_launch_s * 1e3,
                      "step_time_per_sweep_ms": step_sweep_ms},
         "gpu_launches": launches,
