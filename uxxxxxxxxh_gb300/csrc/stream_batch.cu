@@ -1,9 +1,10 @@
 // Persistent batched sweep: one launch advances every grid of a batch by one
 // timestep, whatever its extents, stencil shape or precision.
 //
-// The host cuts every grid into work items (tile x z-chunk), lists them, and
-// launches one CTA per resident slot (SMs x occupancy).  Each CTA walks the
-// list with a fixed stride, copies the item's grid arguments (pointers,
+// The host cuts every grid into work items (tile x z-chunk), lists them
+// costliest first, and launches one CTA per resident slot (SMs x occupancy).
+// Each CTA takes the next item from a per-launch counter, copies the item's
+// grid arguments (pointers,
 // strides, domain, coefficients) into shared memory and runs the streaming
 // sweep body of that grid's variant (stream_item), chosen from a compile-time
 // pack of variants: all 12 shapes in float-pair FP64 and native FP32 in one
@@ -16,13 +17,21 @@
 namespace uhs {
 namespace {
 
-// 256-thread variants: rank 3 star and r1 box 32x32 (VY 4), r2/r3 box 32x16
-// (VY 2, PD 2), rank 2 rows of 256.
+// 256-thread variants: rank 3 r1 box and FP32 r1 star 32x32 (VY 4); other
+// rank 3 stars 32x16 (VY 2: a VY 4 register queue of float pairs or doubles
+// spills at the pack's 80 registers); r2/r3 box 32x16 (VY 2, PD 2); rank 2
+// rows of 256.  batch_tile() gives the host the same tile.
+template <int SHAPE, int R, int ST>
+constexpr bool batch_vy2() {
+    return (SHAPE == kBox3 && R >= 2) || (SHAPE == kStar3 && (ST != kStF32 || R >= 2));
+}
 template <int SHAPE, int R, int ST, int AR>
 using BV = std::conditional_t<
     is_rank2_shape(SHAPE), StreamCfg<SHAPE, R, ST, AR, kLdCpAsync, 256, 1, 1, 4>,
     std::conditional_t<(SHAPE == kBox3 && R >= 2), StreamCfg<SHAPE, R, ST, AR, kLdCpAsync, 32, 8, 2, 2>,
-                       StreamCfg<SHAPE, R, ST, AR, kLdCpAsync, 32, 8, 4, 3>>>;
+                       std::conditional_t<batch_vy2<SHAPE, R, ST>(),
+                                          StreamCfg<SHAPE, R, ST, AR, kLdCpAsync, 32, 8, 2, 3>,
+                                          StreamCfg<SHAPE, R, ST, AR, kLdCpAsync, 32, 8, 4, 3>>>>;
 
 template <int ST, int AR>
 struct Twelve {
@@ -69,14 +78,23 @@ __device__ __forceinline__ void run_kind(Pack<Cs...>, int kind, const BatchArgs 
     ((kind == k++ ? item_call<Cs>(a, bx, by, bz, smem) : (void)0), ...);
 }
 
+// Items are fetched dynamically (one atomicAdd per item on a per-launch
+// counter): the host orders the list by decreasing estimated cost, so the
+// long items start first and the launch ends on short ones.
 template <class P>
 __global__ void __launch_bounds__(256, 3) k_stream_batch(const BatchGrid *__restrict__ grids,
-                                                      const int4 *__restrict__ items, int n_items, int dir) {
+                                                      const int4 *__restrict__ items, int n_items, int dir,
+                                                      int *__restrict__ counter) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ BatchArgs sa;
     __shared__ int skind;
+    __shared__ int snext;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    for (;;) {
+        if (tid == 0) snext = atomicAdd(counter, 1);
+        __syncthreads();
+        const int it = snext;
+        if (it >= n_items) break;
         const int4 w = items[it];
         const uint4 *src = reinterpret_cast<const uint4 *>(&grids[w.x].dir[dir]);
         uint4 *dst = reinterpret_cast<uint4 *>(&sa);
@@ -123,14 +141,18 @@ int batch_kind(int pack, int shape, int R, int st, int ar) {
     return -1;
 }
 
-void batch_tile(int shape, int R, int *bx, int *by, int *zchunk) {
+// 32-plane z-chunks: longer chunks re-read fewer halo planes but give fewer,
+// longer items; on GB300 16, 24, 32 and 16(R+1) planes timed within 2 % on
+// the 64-grid suite, and 32 was fastest.
+void batch_tile(int shape, int R, int st, int *bx, int *by, int *zchunk) {
     if (is_rank2_shape(shape)) {
         *bx = 256;
         *by = 1;
         *zchunk = 128;
     } else {
+        const bool vy2 = (shape == kBox3 && R >= 2) || (shape == kStar3 && (st != kStF32 || R >= 2));
         *bx = 32;
-        *by = (shape == kBox3 && R >= 2) ? 16 : 32;
+        *by = vy2 ? 16 : 32;
         *zchunk = 32;
     }
 }
@@ -140,12 +162,12 @@ cudaError_t batch_prepare(int pack, BatchPackInfo *info) {
 }
 
 cudaError_t batch_launch(int pack, const BatchGrid *grids, const int4 *items, int n_items, int dir, int ctas,
-                         cudaStream_t st) {
+                         int *counter, cudaStream_t st) {
     if (n_items <= 0) return cudaSuccess;
     if (pack == kPackMain)
-        k_stream_batch<MainPack><<<ctas, dim3(32, 8), MainPack::SMEM, st>>>(grids, items, n_items, dir);
+        k_stream_batch<MainPack><<<ctas, dim3(32, 8), MainPack::SMEM, st>>>(grids, items, n_items, dir, counter);
     else
-        k_stream_batch<NativePack><<<ctas, dim3(32, 8), NativePack::SMEM, st>>>(grids, items, n_items, dir);
+        k_stream_batch<NativePack><<<ctas, dim3(32, 8), NativePack::SMEM, st>>>(grids, items, n_items, dir, counter);
     count_launch();
     return cudaGetLastError();
 }
@@ -171,7 +193,7 @@ void batch_fill_args(BatchArgs *a, const StreamCall &c, int nt) {
     a->shift = 0;
     a->pair_loads = c.pair_loads;
     a->err = c.err;
-    fill_coefs(a->cd, a->ch, a->cl, a->cl_sum, c.coef, nt < kBatchNT ? nt : kBatchNT, c.shape, c.R);
+    fill_coefs(a->cd, a->chl, a->cl_sum, c.coef, nt < kBatchNT ? nt : kBatchNT, c.shape, c.R);
 }
 
 }  // namespace uhs

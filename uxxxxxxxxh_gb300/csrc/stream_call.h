@@ -34,7 +34,7 @@ struct StreamArgs {
     int pair_loads;  // cp.async of 4-byte elements in 8-byte pairs (origin and pitches even)
     unsigned *err;
     double cd[NT];
-    float ch[NT], cl[NT];
+    float2 chl[NT];  // float rounding of each coefficient and its rounding error (hi, lo)
     // Float grids: sum of the coefficients' float rounding errors (c - ch),
     // per pass (sep: z, y, x; otherwise [0]); applied once per point to the
     // centre value so the sweep keeps the FP64 coefficients' sum.
@@ -43,15 +43,14 @@ struct StreamArgs {
 
 // Coefficients in the three forms the kernels use, plus the per-pass sums of
 // the float rounding errors (separable shapes: passes z | y | x, D each).
-inline void fill_coefs(double *cd, float *ch, float *cl, float *cl_sum, const double *coef, int nt, int shape, int R) {
+inline void fill_coefs(double *cd, float2 *chl, float *cl_sum, const double *coef, int nt, int shape, int R) {
     const int D = 2 * R + 1;
     double sums[3] = {0.0, 0.0, 0.0};
     for (int k = 0; k < nt; ++k) {
         const double v = coef[k];
         const float h = static_cast<float>(v);
         cd[k] = v;
-        ch[k] = h;
-        cl[k] = static_cast<float>(v - static_cast<double>(h));
+        chl[k] = make_float2(h, static_cast<float>(v - static_cast<double>(h)));
         const int pass = (shape == kSep3 || shape == kSep2) ? k / D : 0;
         sums[pass < 3 ? pass : 2] += v - static_cast<double>(h);
     }
@@ -142,10 +141,12 @@ struct BatchPackInfo {
 // Variant index of (shape, R, storage, arithmetic) in a pack, or -1.
 int batch_kind(int pack, int shape, int R, int st, int ar);
 // Tile and z-chunk every batch item of that variant uses.
-void batch_tile(int shape, int R, int *bx, int *by, int *zchunk);
+void batch_tile(int shape, int R, int st, int *bx, int *by, int *zchunk);
 cudaError_t batch_prepare(int pack, BatchPackInfo *info);
+// CTAs take items in list order through *counter (zero before the launch):
+// a list ordered by decreasing cost then ends with the cheapest items.
 cudaError_t batch_launch(int pack, const BatchGrid *grids, const int4 *items, int n_items, int dir, int ctas,
-                         cudaStream_t st);
+                         int *counter, cudaStream_t st);
 // Temporal fusion (stream_fused.cu): K in {2, 4} steps of the 3D 7-point
 // star per pass; and the halo comparison that gates it.
 cudaError_t launch_fused(const StreamCall &c, int K);

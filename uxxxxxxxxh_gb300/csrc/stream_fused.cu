@@ -47,7 +47,7 @@ struct FusedArgs {
     int zchunk;
     unsigned *err;
     double cd[7];
-    float ch[7], cl[7];
+    float2 chl[7];
     float cl_sum;
 };
 
@@ -59,7 +59,7 @@ struct FArith<C, kArNative> {  // float grids: centre correction as in Arith (st
     static constexpr bool F32 = std::is_same_v<T, float>;
     using Acc = T;
     __device__ static T c(const FusedArgs &a, int k) {
-        if constexpr (F32) return a.ch[k];
+        if constexpr (F32) return a.chl[k].x;
         else return a.cd[k];
     }
     __device__ static void first(Acc &s, const FusedArgs &a, int k, T v) { s = c(a, k) * v; }
@@ -73,8 +73,10 @@ struct FArith<C, kArNative> {  // float grids: centre correction as in Arith (st
 template <class C>
 struct FArith<C, kArDf32> {
     using Acc = df;
-    __device__ static void first(Acc &s, const FusedArgs &a, int k, float2 v) { df_mul(s, a.ch[k], a.cl[k], v); }
-    __device__ static void add(Acc &s, const FusedArgs &a, int k, float2 v) { df_fma(s, a.ch[k], a.cl[k], v); }
+    __device__ static void first(Acc &s, const FusedArgs &a, int k, float2 v) {
+        df_mul(s, a.chl[k].x, a.chl[k].y, v);
+    }
+    __device__ static void add(Acc &s, const FusedArgs &a, int k, float2 v) { df_fma(s, a.chl[k].x, a.chl[k].y, v); }
     __device__ static void centre(Acc &, const FusedArgs &, float2) {}
     __device__ static float2 level(const Acc &s) { return renorm(s); }
     __device__ static void store(double *p, const Acc &s) { *p = join_f64(s.h, s.l); }
@@ -222,7 +224,7 @@ cudaError_t launch_fused_t(const StreamCall &c) {
     a.zchunk = c.zchunk;
     a.err = c.err;
     float sums[3];
-    fill_coefs(a.cd, a.ch, a.cl, sums, c.coef, 7, c.shape, c.R);
+    fill_coefs(a.cd, a.chl, sums, c.coef, 7, c.shape, c.R);
     a.cl_sum = sums[0];
     static bool attr = false;
     if (!attr) {

@@ -152,13 +152,14 @@ __device__ __forceinline__ void tma_load_3d(void *smem, const CUtensorMap *map, 
 // ---- arithmetic policies -----------------------------------------------
 // Coefficient reads.  Kernel parameters (StreamArgs) sit in the constant
 // bank and feed the FMA directly.  The batched kernel keeps each item's
-// arguments in shared memory (BatchArgs); for stencils of more than
-// 32 terms it reads every coefficient where it is used, through a volatile
-// load the compiler cannot hoist out of the plane loop (hoisting 343 of them
-// would exhaust the register file).
+// arguments in shared memory (BatchArgs) and reads every coefficient where
+// it is used, through a volatile load the compiler cannot hoist out of the
+// plane loop: hoisted, even a 13-term star's float pairs push the batched
+// kernel's item functions (80 registers at 3 CTAs of 256 threads) into
+// spilling, and 343 of them would exhaust the register file.
 template <class C, class Args>
 __device__ __forceinline__ double coef_d(const Args &a, int k) {
-    if constexpr (std::is_same_v<Args, BatchArgs> && (C::NT > 32)) {
+    if constexpr (std::is_same_v<Args, BatchArgs>) {
         double v;
         asm volatile("ld.shared.f64 %0, [%1];" : "=d"(v) : "r"((unsigned)__cvta_generic_to_shared(&a.cd[k])));
         return v;
@@ -168,12 +169,26 @@ __device__ __forceinline__ double coef_d(const Args &a, int k) {
 }
 template <class C, class Args>
 __device__ __forceinline__ float coef_f(const Args &a, const float *p) {
-    if constexpr (std::is_same_v<Args, BatchArgs> && (C::NT > 32)) {
+    if constexpr (std::is_same_v<Args, BatchArgs>) {
         float v;
         asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"((unsigned)__cvta_generic_to_shared(p)));
         return v;
     } else {
         return *p;
+    }
+}
+
+// The (hi, lo) float pair of coefficient k in one 8-byte read.
+template <class C, class Args>
+__device__ __forceinline__ float2 coef_f2(const Args &a, int k) {
+    if constexpr (std::is_same_v<Args, BatchArgs>) {
+        float2 v;
+        asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];"
+                     : "=f"(v.x), "=f"(v.y)
+                     : "r"((unsigned)__cvta_generic_to_shared(&a.chl[k])));
+        return v;
+    } else {
+        return a.chl[k];
     }
 }
 
@@ -195,7 +210,7 @@ struct Arith<C, kArNative> {
     template <class Args>
     __device__ static __forceinline__ TS coef(const Args &a, int k) {
         if constexpr (!F32) return coef_d<C>(a, k);
-        else return coef_f<C>(a, &a.ch[k]);
+        else return coef_f<C>(a, &a.chl[k].x);
     }
     template <class Args>
     __device__ static __forceinline__ void first(Acc &acc, const Args &a, int k, TS v) {
@@ -218,11 +233,13 @@ struct Arith<C, kArDf32> {
     using Acc = df;
     template <class Args>
     __device__ static __forceinline__ void first(Acc &acc, const Args &a, int k, float2 v) {
-        df_mul(acc, coef_f<C>(a, &a.ch[k]), coef_f<C>(a, &a.cl[k]), v);
+        const float2 c = coef_f2<C>(a, k);
+        df_mul(acc, c.x, c.y, v);
     }
     template <class Args>
     __device__ static __forceinline__ void add(Acc &acc, const Args &a, int k, float2 v) {
-        df_fma(acc, coef_f<C>(a, &a.ch[k]), coef_f<C>(a, &a.cl[k]), v);
+        const float2 c = coef_f2<C>(a, k);
+        df_fma(acc, c.x, c.y, v);
     }
     __device__ static __forceinline__ void store(typename C::TS *p, const Acc &acc) {
         if constexpr (C::ST == kStF64) *p = join_f64(acc.h, acc.l);

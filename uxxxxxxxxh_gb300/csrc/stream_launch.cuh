@@ -33,7 +33,7 @@ cudaError_t launch_cfg(const StreamCall &c) {
     a.shift = c.shift;
     a.pair_loads = c.pair_loads;
     a.err = c.err;
-    fill_coefs(a.cd, a.ch, a.cl, a.cl_sum, c.coef, C::NT, c.shape, c.R);
+    fill_coefs(a.cd, a.chl, a.cl_sum, c.coef, C::NT, c.shape, c.R);
     const int64_t nz = c.ub[0] - c.lb[0], ny = c.ub[1] - c.lb[1], nx = c.ub[2] - c.lb[2];
     if (!c.occ_out && (nz <= 0 || ny <= 0 || nx <= 0)) return cudaSuccess;
     static bool attr_set = false;

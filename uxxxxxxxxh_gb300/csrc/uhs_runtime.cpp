@@ -770,8 +770,19 @@ int prepare_error_norms(const uhs_stencil_desc *d, const uhs_memref *x, const uh
 // ---------------------------------------------------------------------------
 struct BatchGridHost {
     int pack, kind, T, order;
+    int bx, by, zc;    // item tile and z-chunk
     int64_t items;
+    double item_cost;  // estimated cost of one item, for the list order
 };
+
+// Relative cost of one work item: points per item x (per-point overhead +
+// terms x per-term cost of the arithmetic).  Per-term costs follow the
+// measured rates of the streaming kernels (FP32 FFMA 1, float pairs about
+// 6 FP32 operations' worth, native FP64 bound by the FP64 pipe).
+static double batch_item_cost(int bx, int by, int zc, int nterms, int st, int ar) {
+    const double per_term = st == kStF32 ? 1.0 : ar == kArDf32 ? 6.0 : 14.0;
+    return static_cast<double>(bx) * by * zc * (20.0 + per_term * nterms);
+}
 
 struct uhs_batch_impl {
     int dev = 0;
@@ -780,6 +791,7 @@ struct uhs_batch_impl {
     int64_t launches = 0, items0 = 0;
     BatchGrid *d_grids = nullptr;
     int4 *d_items[kNumPacks] = {nullptr, nullptr};
+    int *d_counters = nullptr;  // one item counter per (timestep, pack), zeroed at each replay
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -789,6 +801,7 @@ static void batch_free(uhs_batch_impl *b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     if (b->d_grids) cudaFree(b->d_grids);
+    if (b->d_counters) cudaFree(b->d_counters);
     for (auto *p : b->d_items)
         if (p) cudaFree(p);
     delete b;
@@ -853,8 +866,7 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
         c.ub[2] = sp.ub[2];
         c.err = err;
         int bx, by, zc;
-        batch_tile(pl.shape, pl.R, &bx, &by, &zc);
-        c.zchunk = zc;
+        batch_tile(pl.shape, pl.R, pl.st, &bx, &by, &zc);
         const int eb = sp.dtype == UHS_F32 ? 4 : 8;
         for (int d = 0; d < 2; ++d) {
             c.in = kernel_view(sp, d == 0 ? va : vb);
@@ -866,16 +878,43 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
             batch_fill_args(&host[i].dir[d], c, static_cast<int>(pl.coef.size()));
         }
         host[i].kind = kind;
-        const int64_t tx = (c.ub[2] - c.lb[2] + bx - 1) / bx, ty = (c.ub[1] - c.lb[1] + by - 1) / by,
-                      tz = (c.ub[0] - c.lb[0] + zc - 1) / zc;
-        info[i] = BatchGridHost{pack, kind, descs[i].iterations, i, tx * ty * tz};
-        if (tx * ty * tz > (int64_t(1) << 28)) return set_error(UHS_EUNSUPPORTED, "program %d has too many tiles", i);
+        info[i] = BatchGridHost{pack, kind, descs[i].iterations, i, bx, by, zc, 0,
+                                batch_item_cost(bx, by, 1, static_cast<int>(pl.coef.size()), pl.st, pl.ar)};
+    }
+    // z-chunks: the batch's estimated work shared by every resident CTA sets
+    // a target item cost; grids whose 32-plane items would exceed a quarter of
+    // a CTA's share get shorter chunks (down to 8 planes), so no single long
+    // item holds up the end of a timestep.
+    {
+        double work = 0.0;
+        for (int i = 0; i < n; ++i) {
+            const BatchArgs &a0 = host[i].dir[0];
+            work += info[i].item_cost * static_cast<double>((a0.ub2 - a0.lb2) * (a0.ub1 - a0.lb1)) /
+                    (static_cast<double>(info[i].bx) * info[i].by) * static_cast<double>(a0.ub0 - a0.lb0);
+        }
+        const double target = work / (4.0 * device_sms() * 3);
+        for (int i = 0; i < n; ++i) {
+            BatchGridHost &g = info[i];
+            int zc = g.zc;
+            while (zc > 8 && g.item_cost * zc > target) zc /= 2;
+            g.zc = zc;
+            g.item_cost *= zc;
+            for (int d = 0; d < 2; ++d) host[i].dir[d].zchunk = zc;
+            const BatchArgs &a0 = host[i].dir[0];
+            const int64_t tx = (a0.ub2 - a0.lb2 + g.bx - 1) / g.bx, ty = (a0.ub1 - a0.lb1 + g.by - 1) / g.by,
+                          tz = (a0.ub0 - a0.lb0 + zc - 1) / zc;
+            g.items = tx * ty * tz;
+            if (g.items > (int64_t(1) << 28)) return set_error(UHS_EUNSUPPORTED, "program %d has too many tiles", i);
+        }
     }
     // Items of each pack, grids in decreasing T so a timestep's active items
-    // are a prefix of the list.
+    // are a prefix of the list; within one T, costliest items first.
     std::vector<int> order(static_cast<size_t>(n));
     for (int i = 0; i < n; ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return info[x].T > info[y].T; });
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        if (info[x].T != info[y].T) return info[x].T > info[y].T;
+        return info[x].item_cost > info[y].item_cost;
+    });
     std::vector<std::vector<int64_t>> prefix(kNumPacks);  // prefix[pack][step] = active items
     int steps = 0;
     for (int i = 0; i < n; ++i) steps = std::max(steps, info[i].T);
@@ -883,14 +922,7 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
     for (int p = 0; p < kNumPacks; ++p) prefix[p].assign(static_cast<size_t>(steps), 0);
     for (int i : order) {
         const int p = info[i].pack;
-        GridView dummy{};
-        (void)dummy;
-        int bx, by, zc;
-        SweepSpec sp;
-        make_spec(&descs[i], &sp);
-        int shape = -1, R = 0;
-        classify(sp, &shape, &R);
-        batch_tile(shape, R, &bx, &by, &zc);
+        const int bx = info[i].bx, by = info[i].by, zc = info[i].zc;
         const BatchArgs &a0 = host[i].dir[0];
         const int64_t tx = (a0.ub2 - a0.lb2 + bx - 1) / bx, ty = (a0.ub1 - a0.lb1 + by - 1) / by,
                       tz = (a0.ub0 - a0.lb0 + zc - 1) / zc;
@@ -930,6 +962,13 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
     B->items0 = 0;
     for (int p = 0; p < kNumPacks; ++p)
         if (steps > 0) B->items0 += prefix[p][0];
+    const size_t n_counters = static_cast<size_t>(steps) * kNumPacks;
+    if (n_counters > 0) {
+        void *q = nullptr;
+        if (cudaMalloc(&q, sizeof(int) * n_counters) != cudaSuccess)
+            return set_error(UHS_ENOMEM, "batch item counters: allocation failed");
+        B->d_counters = static_cast<int *>(q);
+    }
     // Capture the timestep loop.
     if (steps > 0) {
         cudaStream_t cs;
@@ -938,13 +977,15 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
         StreamGuard cg{cs};
         if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
             return set_error(UHS_ECUDA, "graph capture could not start");
-        cudaError_t e = cudaSuccess;
+        // every replay starts by zeroing the item counters (a memset node)
+        cudaError_t e = cudaMemsetAsync(B->d_counters, 0, sizeof(int) * n_counters, cs);
         int64_t launches = 0;
         for (int s = 0; s < steps && e == cudaSuccess; ++s) {
             for (int p = 0; p < kNumPacks && e == cudaSuccess; ++p) {
                 const int64_t m = prefix[p][s];
                 if (m <= 0) continue;
-                e = batch_launch(p, B->d_grids, B->d_items[p], static_cast<int>(m), s & 1, ctas[p], cs);
+                e = batch_launch(p, B->d_grids, B->d_items[p], static_cast<int>(m), s & 1, ctas[p],
+                                 B->d_counters + static_cast<size_t>(s) * kNumPacks + p, cs);
                 ++launches;
             }
         }
