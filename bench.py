@@ -56,6 +56,7 @@ def parse_args():
     p.add_argument("--no-cpu", action="store_true", help="skip the oracle (profiling runs)")
     p.add_argument("--no-fp32", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-tune", action="store_true", help="cfg5: skip the standalone cost-model / exhaustive comparison")
     return p.parse_args()
 
 
@@ -284,7 +285,9 @@ def bench_batch(args, rank: int, world: int, local: int):
     """cfg5: 64 programs across all 12 shapes, FP32 and FP64, 20 timesteps,
     one persistent launch per timestep replayed from a CUDA graph.  Grid data
     is drawn on the device (seeded) -- the batch timing does not depend on it;
-    the parity of batches is covered by tests/test_batch_gpu.py."""
+    the parity of batches is covered by tests/test_batch_gpu.py.  Beside it
+    (unless --no-tune): the same programs launched one by one with launch
+    parameters from the cost model and from exhaustive tuning."""
     import torch
     import uxxxxxxxxh_gb300 as uhs
     from uxxxxxxxxh_gb300.workloads import cfg5_specs
@@ -321,6 +324,7 @@ def bench_batch(args, rank: int, world: int, local: int):
     value = pts * args.steps / (ms * 1e-3) / 1e9
     achieved = byts * args.steps / (ms * 1e-3) / 1e9
     st_ = batch.stats()
+    tuning = None if args.no_tune else standalone_tuning(uhs, specs, A, B, stream, pts)
     line = {"metric": "GStencil/s", "value": value, "unit": "GStencil/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)",
@@ -330,8 +334,52 @@ def bench_batch(args, rank: int, world: int, local: int):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_source": peak_kind},
             "gpu_launches": uhs.launch_count() - n0, "clocks": clk}
+    if tuning:
+        line["standalone"] = tuning
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def standalone_tuning(uhs, specs, A, B, stream, pts):
+    """The same 64 programs launched one by one (T sweeps each), with launch
+    parameters from the shipped cost model (no timing), from its three
+    best-ranked candidates timed, and from exhaustive tuning of each program
+    (the judge).  GStencil/s of one pass over all programs."""
+    import torch
+    from uxxxxxxxxh_gb300.costmodel import CostModel
+    from uxxxxxxxxh_gb300.tuner import Tuner
+    cm = CostModel.default()
+    F = uhs._lib
+    picks = {"mlp": [], "mlp_top3": [], "exhaustive": []}
+    t0 = time.perf_counter()
+    for i, (st, _) in enumerate(specs):
+        picks["mlp"].append(cm.pick(st))
+        picks["mlp_top3"].append(cm.pick_verified(st, A[i], B[i], k=3))
+        picks["exhaustive"].append(Tuner().tune(st, A[i], B[i], push=False)[0])
+    tune_s = time.perf_counter() - t0
+    out = {"tuning_seconds": tune_s}
+    for name, ps in picks.items():
+        qs = [uhs.RunParams(**{**p.__dict__, "flags": F.UHS_FLAG_NO_SYNC | F.UHS_FLAG_NO_TUNE_DB}) for p in ps]
+
+        def one_pass():
+            for i, (st, _) in enumerate(specs):
+                uhs.run(st, A[i], B[i], qs[i], stream=stream)
+        one_pass()
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(2):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            one_pass()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        out[name] = {"gstencil_s": pts / (best * 1e-3) / 1e9, "ms": best}
+    out["mlp_vs_exhaustive"] = out["mlp"]["gstencil_s"] / out["exhaustive"]["gstencil_s"]
+    out["mlp_top3_vs_exhaustive"] = out["mlp_top3"]["gstencil_s"] / out["exhaustive"]["gstencil_s"]
+    return out
 
 
 def main():
