@@ -301,6 +301,7 @@ def bench_batch(args, rank: int, world: int, local: int):
         a = torch.rand(shape, generator=gen, device="cuda", dtype=torch.float64).mul_(2).sub_(1).to(dt)
         A.append(a)
         B.append(a.clone())
+    host0 = None if args.no_cpu else [a.cpu() for a in A]  # initial grids, for the oracle check
     batch = uhs.Batch([s for s, _ in specs], A, B, uhs.RunParams())
     stream = torch.cuda.Stream()
     for _ in range(args.warmup):
@@ -324,6 +325,7 @@ def bench_batch(args, rank: int, world: int, local: int):
     value = pts * args.steps / (ms * 1e-3) / 1e9
     achieved = byts * args.steps / (ms * 1e-3) / 1e9
     st_ = batch.stats()
+    errors = None if args.no_cpu else batch_errors(uhs, batch, specs, A, B, host0, stream)
     tuning = None if args.no_tune else standalone_tuning(uhs, specs, A, B, stream, pts)
     line = {"metric": "GStencil/s", "value": value, "unit": "GStencil/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -334,10 +336,40 @@ def bench_batch(args, rank: int, world: int, local: int):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_source": peak_kind},
             "gpu_launches": uhs.launch_count() - n0, "clocks": clk}
+    if errors:
+        line["error_vs_oracle"] = errors
     if tuning:
         line["standalone"] = tuning
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def batch_errors(uhs, batch, specs, A, B, host0, stream):
+    """One replay of the batch from the initial grids, every grid scored
+    against the FP64 oracle (FP32 grids: the oracle on their float values).
+    Returns the worst relative L2 and max error per element type."""
+    import torch
+    import oracle
+    oracle.set_threads(os.cpu_count() or 1)
+    for a, b, h in zip(A, B, host0):
+        a.copy_(h)
+        b.copy_(h)
+    batch.run(stream)
+    torch.cuda.synchronize()
+    worst = {}
+    t0 = time.perf_counter()
+    for (st, _), a, h in zip(specs, A, host0):
+        x0 = h.double().numpy().reshape(-1).copy()
+        ra, rb = x0.copy(), x0.copy()
+        oracle.iterate_f64(st, ra, rb)
+        e = oracle.error(st, ra, a.double().cpu().numpy().reshape(-1))
+        k = "f32" if st.dtype == uhs.UHS_F32 else "f64"
+        w = worst.setdefault(k, {"grids": 0, "l2_rel": 0.0, "max_rel": 0.0})
+        w["grids"] += 1
+        w["l2_rel"] = max(w["l2_rel"], e["l2_rel"])
+        w["max_rel"] = max(w["max_rel"], e["max_rel"])
+    worst["oracle_seconds"] = time.perf_counter() - t0
+    return worst
 
 
 def standalone_tuning(uhs, specs, A, B, stream, pts):

@@ -131,7 +131,9 @@ typedef struct uhs_params {
 enum {
     UHS_FLAG_NO_SYNC = 1,    /* return without synchronising the stream */
     UHS_FLAG_NO_TUNE_DB = 2, /* ignore the tuner database for this call */
-    UHS_FLAG_NO_FACTOR = 4   /* sweep a separable box term by term, not as 1D passes */
+    UHS_FLAG_NO_FACTOR = 4,  /* sweep a separable box term by term, not as 1D passes */
+    UHS_FLAG_MMA_TMEM_A = 8  /* tensor-core path: stage the A operand in tensor memory
+                                (tcgen05.cp) instead of reading it from shared memory */
 };
 
 /* ---- entry points ------------------------------------------------------ */

@@ -41,12 +41,17 @@ def check_f32(st, a0, params, l2=MMA_L2):
     return e
 
 
-@pytest.mark.parametrize("r,xtile", [(2, 16), (2, 32), (3, 16)])
+TMEM_A = uhs._lib.UHS_FLAG_MMA_TMEM_A
+
+
+# A operand read from shared memory (the default), or staged in tensor memory
+# by tcgen05.cp (flag, 16-column tiles)
+@pytest.mark.parametrize("r,xtile,flags", [(2, 16, 0), (3, 16, 0), (2, 16, TMEM_A), (3, 16, TMEM_A), (2, 32, 0)])
 @pytest.mark.parametrize("T", [1, 2, 6])
-def test_mma_box_matches_oracle(cuda, r, xtile, T):
+def test_mma_box_matches_oracle(cuda, r, xtile, flags, T):
     # 150 rows: two 128-row tiles, the second ragged; 45 columns: ragged x tiles
     st, a0 = f32_case(r, (21, 150, 45), T, 40 + r)
-    p = uhs.RunParams(kernel=MMA, tile_x=xtile)
+    p = uhs.RunParams(kernel=MMA, tile_x=xtile, flags=flags)
     assert uhs.plan(st, params=p).kernel == MMA
     check_f32(st, a0, p)
 
@@ -108,15 +113,20 @@ def test_mma_refusals(cuda):
     assert ei.value.code == uhs._lib.UHS_EINVAL
     with pytest.raises(uhs.UhsError):
         uhs.plan(st, params=uhs.RunParams(kernel=MMA, k_temporal=2))
+    st2, _ = f32_case(2, (8, 8, 16), 2, 73)
+    with pytest.raises(uhs.UhsError) as ei:
+        uhs.plan(st2, params=uhs.RunParams(kernel=MMA, tile_x=32, flags=TMEM_A))
+    assert ei.value.code == uhs._lib.UHS_EINVAL
     stars, _ = random_case(3, 2, "star", (8, 8, 16), 2, 72, dtype=uhs.UHS_F32)
     with pytest.raises(uhs.UhsError):
         uhs.plan(stars, params=uhs.RunParams(kernel=MMA))
 
 
-def test_mma_many_planes_per_cta_and_tiny_grid(cuda):
+@pytest.mark.parametrize("flags", [0, TMEM_A])
+def test_mma_many_planes_per_cta_and_tiny_grid(cuda, flags):
     """More plane tiles than CTAs (each CTA walks several segments) and a grid
     smaller than one tile."""
     st, a0 = f32_case(2, (300, 20, 20), 2, 80)
-    check_f32(st, a0, uhs.RunParams(kernel=MMA))
+    check_f32(st, a0, uhs.RunParams(kernel=MMA, flags=flags))
     st2, b0 = f32_case(3, (3, 5, 7), 2, 81)
-    check_f32(st2, b0, uhs.RunParams(kernel=MMA))
+    check_f32(st2, b0, uhs.RunParams(kernel=MMA, flags=flags))

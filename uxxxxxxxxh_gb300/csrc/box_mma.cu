@@ -29,6 +29,14 @@
 // kernel is persistent: each CTA takes a contiguous range of (tile, z) plane
 // tiles, so the SMs get equal shares whatever the grid's shape.
 //
+// Variant (UHS_FLAG_MMA_TMEM_A): the A operand staged in tensor memory, D
+// row-shifted hi/lo copies per input plane made by tcgen05.cp, so the MMAs
+// read only the small B from shared memory.  Tensor memory holds one set of
+// copies beside the accumulators (464 of 512 columns for R = 3), so a plane's
+// copies wait for the previous plane's MMAs.  Measured on GB300 it is slower
+// (15 vs 20 GStencil/s, 343-point box): the MMA instructions themselves, at
+// N = 16, not the operand reads, set the pace.
+//
 // Every wait is bounded: a wait that runs out sets the device error word,
 // waits (bounded) for its own MMAs, frees its tensor memory and returns.
 #include <cuda_runtime.h>
@@ -57,7 +65,7 @@ struct MmaArgs {
     double cd[343];
 };
 
-template <int R, int NS>
+template <int R, int NS, bool ATMEM>
 struct MmaCfg {
     static constexpr int D = 2 * R + 1;
     static constexpr int YR = kMmaM + 2 * R;  // staged rows
@@ -73,13 +81,17 @@ struct MmaCfg {
     static constexpr uint32_t BAR_OFF = B_OFF + D * D * BPAIR;
     static constexpr uint32_t SMEM = BAR_OFF + 32;
     static constexpr int NSLOT = 2 * R + 2;
-    static constexpr int COLS = NSLOT * XT;
+    // A in tensor memory: D row-shifted copies of the staged plane, each
+    // 24 hi + 24 lo columns, after the accumulators.
+    static constexpr int ACOL0 = NSLOT * XT;
+    static constexpr int COLS = ATMEM ? ACOL0 + D * 48 : NSLOT * XT;
     static constexpr uint32_t NCOLS = COLS <= 32 ? 32 : COLS <= 64 ? 64 : COLS <= 128 ? 128 : COLS <= 256 ? 256 : 512;
     static constexpr int NE = YR * XW;
     static constexpr int NQ = (NE + kMmaThreads - 1) / kMmaThreads;
     // instruction descriptor: D f32, A/B tf32, both K-major, N = 16, M = 128
     static constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
     static_assert(COLS <= 512, "tensor memory holds 512 columns");
+    static_assert(!ATMEM || NS == 1, "A in tensor memory: one 16-column tile");
     static_assert(SMEM <= 232448, "shared memory per CTA");
     static_assert(D * D * D * 8 <= STG, "coefficient table fits in stage 0");
 };
@@ -105,6 +117,19 @@ __device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uin
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
         " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
         "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+// A from tensor memory (lanes = rows, columns = K), B from shared memory.
+__device__ __forceinline__ void mma_tf32_ta(uint32_t d, uint32_t a_tmem, uint64_t b, uint32_t idesc,
+                                            uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d),
+        "r"(a_tmem), "l"(b), "r"(idesc), "r"(acc));
+}
+// Shared memory (128 rows x 32 bytes, canonical layout) -> tensor memory
+// lanes 0-127, 8 columns.
+__device__ __forceinline__ void tmem_cp_128x256b(uint32_t taddr, uint64_t src) {
+    asm volatile("tcgen05.cp.cta_group::1.128x256b [%0], %1;\n" ::"r"(taddr), "l"(src) : "memory");
 }
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
@@ -160,10 +185,44 @@ __device__ __forceinline__ void store_plane(const float (&v)[C::NQ], unsigned ch
     }
 }
 
-// All MMAs of input plane zi (one thread).
-template <class C, int R, int NS>
+// All MMAs of input plane zi (one thread).  With A in tensor memory the
+// plane's D row-shifted hi/lo copies are made first (tcgen05.cp, executed
+// before the MMAs issued after them by the same thread).
+template <class C, int R, int NS, bool ATMEM>
 __device__ __forceinline__ void issue_plane(uint32_t st_addr, uint32_t b_addr, uint32_t tbase, int zi, int zs,
                                             int ze) {
+    if constexpr (ATMEM) {
+#pragma unroll 1
+        for (int dyi = 0; dyi < C::D; ++dyi)
+#pragma unroll
+            for (int half = 0; half < 2; ++half)
+#pragma unroll
+                for (int c3 = 0; c3 < 3; ++c3)
+                    tmem_cp_128x256b(tbase + C::ACOL0 + (dyi * 2 + half) * 24 + 8 * c3,
+                                     sdesc(st_addr + half * C::HALF + (2u * c3) * C::LBO_A + dyi * 16u, C::LBO_A,
+                                           128));
+#pragma unroll 1
+        for (int dzi = 0; dzi < C::D; ++dzi) {
+            const int zo = zi + R - dzi;
+            if (zo < zs || zo >= ze) continue;
+            const uint32_t dcol = tbase + static_cast<uint32_t>((zo - zs) % C::NSLOT) * C::XT;
+#pragma unroll 1
+            for (int dyi = 0; dyi < C::D; ++dyi) {
+                const uint64_t bh = sdesc(b_addr + static_cast<uint32_t>(dzi * C::D + dyi) * C::BPAIR, 256, 128);
+                const uint64_t bl = bh + (C::BMAT >> 4);
+                const uint32_t ah = tbase + C::ACOL0 + dyi * 48, al = ah + 24;
+#pragma unroll
+                for (int ks = 0; ks < 3; ++ks) {
+                    const uint64_t kb = (2u * ks * 256u) >> 4;
+                    const uint32_t acc = (dzi == 0 && dyi == 0 && ks == 0) ? 0u : 1u;
+                    mma_tf32_ta(dcol, ah + 8 * ks, bh + kb, C::IDESC, acc);
+                    mma_tf32_ta(dcol, al + 8 * ks, bh + kb, C::IDESC, 1u);
+                    mma_tf32_ta(dcol, ah + 8 * ks, bl + kb, C::IDESC, 1u);
+                }
+            }
+        }
+        return;
+    }
 #pragma unroll 1
     for (int dzi = 0; dzi < C::D; ++dzi) {
         const int zo = zi + R - dzi;  // dz = dzi - R, zo = zi - dz
@@ -223,9 +282,9 @@ __device__ void record_timeout(const MmaArgs &a, int zi, int stage, unsigned pha
     a.err[7] = phase;
 }
 
-template <int R, int NS>
+template <int R, int NS, bool ATMEM>
 __global__ void __launch_bounds__(kMmaThreads, 1) k_box_mma(const __grid_constant__ MmaArgs a) {
-    using C = MmaCfg<R, NS>;
+    using C = MmaCfg<R, NS, ATMEM>;
     extern __shared__ __align__(1024) unsigned char smem[];
     const int tid = threadIdx.x, warp = tid >> 5;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + C::BAR_OFF);
@@ -300,7 +359,13 @@ __global__ void __launch_bounds__(kMmaThreads, 1) k_box_mma(const __grid_constan
             __syncthreads();
             if (tid == 0) {
                 tc_fence_after();
-                issue_plane<C, R, NS>(sbase + s * C::STG, b_addr, tbase, zi, zs, ze);
+                // A in tensor memory is single-buffered: plane i's copies
+                // overwrite what plane i-1's MMAs read, so they wait for
+                // those MMAs (the drain below waits on the same phase).
+                bool aok = true;
+                if constexpr (ATMEM)
+                    if (i >= 1) aok = mbar_wait(&bar[s ^ 1], ph[s ^ 1]);
+                if (aok) issue_plane<C, R, NS, ATMEM>(sbase + s * C::STG, b_addr, tbase, zi, zs, ze);
                 mma_commit(&bar[s]);
             }
             if (i >= 1) {
@@ -340,10 +405,10 @@ __global__ void __launch_bounds__(kMmaThreads, 1) k_box_mma(const __grid_constan
     }
 }
 
-template <int R, int NS>
+template <int R, int NS, bool ATMEM>
 cudaError_t launch_t(const MmaCall &c) {
-    using C = MmaCfg<R, NS>;
-    auto kern = k_box_mma<R, NS>;
+    using C = MmaCfg<R, NS, ATMEM>;
+    auto kern = k_box_mma<R, NS, ATMEM>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
     if (e != cudaSuccess) return e;
     int occ = 0;
@@ -387,9 +452,14 @@ cudaError_t launch_t(const MmaCall &c) {
 }  // namespace
 
 cudaError_t launch_box_mma(const MmaCall &c) {
-    if (c.R == 3 && c.xtile == 16) return launch_t<3, 1>(c);
-    if (c.R == 2 && c.xtile == 16) return launch_t<2, 1>(c);
-    if (c.R == 2 && c.xtile == 32) return launch_t<2, 2>(c);
+    if (c.a_tmem) {
+        if (c.R == 3 && c.xtile == 16) return launch_t<3, 1, true>(c);
+        if (c.R == 2 && c.xtile == 16) return launch_t<2, 1, true>(c);
+        return cudaErrorInvalidValue;
+    }
+    if (c.R == 3 && c.xtile == 16) return launch_t<3, 1, false>(c);
+    if (c.R == 2 && c.xtile == 16) return launch_t<2, 1, false>(c);
+    if (c.R == 2 && c.xtile == 32) return launch_t<2, 2, false>(c);
     return cudaErrorInvalidValue;
 }
 

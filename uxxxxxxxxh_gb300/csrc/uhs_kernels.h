@@ -74,6 +74,7 @@ struct MmaCall {
     int64_t lb[3], ub[3];
     int R;
     int xtile;
+    int a_tmem;  // 1: A operand staged in tensor memory (16-column tiles only)
     const double *coef;
     unsigned *err;
     cudaStream_t stream;

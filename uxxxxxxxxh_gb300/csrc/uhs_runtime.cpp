@@ -185,6 +185,7 @@ struct Plan {
     std::vector<double> coef;  // coef_slot order
     bool auto_df32 = false;    // df32 chosen by UHS_ARITH_AUTO, subject to range_ok()
     bool factored = false;     // separable box run as 1D passes
+    bool a_tmem = false;       // tensor-core path: A operand staged in tensor memory
 };
 
 static int device_sms() {
@@ -330,7 +331,8 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
         if (arith != UHS_ARITH_FMA)
             return set_error(UHS_EUNSUPPORTED, "the tensor-core path computes in split-tf32 FMA arithmetic");
         if (cfg.k_temporal > 1) return set_error(UHS_EUNSUPPORTED, "the tensor-core path sweeps one step per pass");
-        int xt = cfg.tile_x > 0 ? cfg.tile_x : (R == 2 ? 32 : 16);
+        const bool want_tmem_a = (p->flags & UHS_FLAG_MMA_TMEM_A) != 0;
+        int xt = cfg.tile_x > 0 ? cfg.tile_x : (R == 2 && !want_tmem_a ? 32 : 16);
         if (!(xt == 16 || (xt == 32 && R == 2)))
             return set_error(UHS_EINVAL, "tensor-core tiles are 16 columns wide (32 for radius 2), got %d", xt);
         if (view.s[0] >= (int64_t(1) << 31) || view.n[0] >= (int64_t(1) << 31))
@@ -344,6 +346,9 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
         pl->st = kStF32;
         pl->ar = kArNative;
         pl->tile = xt;
+        if (want_tmem_a && xt != 16)
+            return set_error(UHS_EINVAL, "the tensor-memory A operand takes 16-column tiles");
+        pl->a_tmem = want_tmem_a;
         pl->coef.assign(nterms_of(shape, R), 0.0);
         for (int k = 0; k < sp.nterms; ++k) pl->coef[coef_slot_rt(shape, R, sp.dz[k], sp.dy[k], sp.dx[k])] += sp.coef[k];
         return UHS_OK;
@@ -532,6 +537,7 @@ static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in,
         }
         m.R = pl.R;
         m.xtile = pl.tile;
+        m.a_tmem = pl.a_tmem ? 1 : 0;
         m.coef = pl.coef.data();
         m.stream = st;
         int dev = 0;
