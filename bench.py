@@ -17,7 +17,7 @@ Reported (one JSON line, rank 0):
   cpu_baseline  the oracle's restatement of the reference's serial loops on
              this host's cores, on a bounded sample of the same workload
   fp32       the same workload on FP32 grids, with its L2 error against the
-             FP64 oracle (the north-star's FP32-vs-FP64 comparison)
+             FP64 oracle (the FP32-vs-FP64 comparison)
 Inputs (1.09 GB per grid) are larger than the 129 MB L2, so no flush is
 needed between timed iterations.
 
@@ -376,7 +376,7 @@ def standalone_tuning(uhs, specs, A, B, stream, pts):
     """The same 64 programs launched one by one (T sweeps each), with launch
     parameters from the shipped cost model (no timing), from its three
     best-ranked candidates timed, and from exhaustive tuning of each program
-    (the judge).  GStencil/s of one pass over all programs."""
+    (the yardstick).  GStencil/s of one pass over all programs."""
     import torch
     from uxxxxxxxxh_gb300.costmodel import CostModel
     from uxxxxxxxxh_gb300.tuner import Tuner

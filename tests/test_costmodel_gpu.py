@@ -2,7 +2,7 @@
 (uxxxxxxxxh_gb300/data/costmodel.json, trained by tuner_study on GB300
 timings of programs drawn from seed 101) ranks the launch candidates of
 programs drawn from another seed, which it never saw; each program is also
-tuned exhaustively (the judge).  Compared with the methods without it:
+tuned exhaustively (the yardstick).  Compared with the methods without it:
 
 * an uninformed pick (the median candidate): the network's pick is faster;
 * exhaustive tuning: the network's three best-ranked candidates, timed

@@ -1,5 +1,5 @@
 """The MLP's CPU oracle (oracle/mlp_oracle.py) against finite differences,
-so that it can in turn judge the GPU kernels' gradients."""
+so that it can in turn check the GPU kernels' gradients."""
 import numpy as np
 
 from oracle import mlp_oracle

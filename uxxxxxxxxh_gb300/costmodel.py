@@ -7,7 +7,7 @@ The network is the library's MLP (include/uhs.h, uhs_mlp_*): 24 features
 and Adam kernels on the tuner's timing records (tuner.Tuner.records).  Target:
 log(ns per point), standardised.  pick() runs the network over every
 candidate of a program and returns the one it predicts fastest; exhaustive
-tuning (tuner.Tuner.tune) stays the fallback and the judge of the model's
+tuning (tuner.Tuner.tune) stays the fallback and the yardstick of the model's
 regret.
 """
 from __future__ import annotations

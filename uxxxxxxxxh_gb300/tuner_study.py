@@ -1,4 +1,4 @@
-"""Train the learned cost model on the tuner's own GB300 timings and judge its
+"""Train the learned cost model on the tuner's own GB300 timings and measure its
 picks against exhaustive tuning.
 
     python -m uxxxxxxxxh_gb300.tuner_study [--train N] [--test M] [--out result.json]
@@ -10,7 +10,7 @@ picks against exhaustive tuning.
 2. The network (costmodel.CostModel, the library's MLP kernels) is trained
    on the GPU on those records.
 3. M held-out programs from another seed, at least one per shape and element
-   type, are tuned exhaustively (the judge).  For each: the exhaustive best,
+   type, are tuned exhaustively (the yardstick).  For each: the exhaustive best,
    the model's pick and the planner's default (no tuner database) are
    compared by their measured throughput, and so is the model's top-3
    verified pick (the fastest of its three best-ranked candidates, timed).
@@ -75,8 +75,8 @@ def run(n_train: int, n_test: int, reps: int, epochs: int, out: str | None, mode
     rows = []
     for st in draw_programs(n_test, seed + 1, cover=True):
         a, b = device_grids(st)
-        judge = Tuner()
-        _, results = judge.tune(st, a, b, reps=reps, push=False)
+        exhaustive = Tuner()
+        _, results = exhaustive.tune(st, a, b, reps=reps, push=False)
         best_p = min(results, key=lambda r: r[0])[1]
         pick = cm.pick(st)
         pick3 = cm.pick_verified(st, a, b, k=3, reps=reps)
