@@ -272,6 +272,15 @@ int uhs_mlp_train(uhs_mlp *m, const float *x, const float *y, int32_t n, int32_t
 /* Number of kernels this library launched since load (diagnostics). */
 int64_t uhs_launch_count(void);
 
+/* Diagnostics: exercise the failure-reporting path.  Launches one CTA whose
+ * mbarrier wait can never complete, bounded at `cycles` SM clocks (1 to 2^31;
+ * 2^31 is the sweep kernels' bound, about one second at 2 GHz).  When the
+ * bound runs out the kernel records a timeout in the device status word the
+ * way the sweep kernels' bounded waits do and returns normally -- nothing
+ * faults and the device stays usable.  Returns UHS_ETIMEOUT with the message
+ * the sweeps would give, after the stream drained. */
+int uhs_probe_wait_timeout(int64_t cycles, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

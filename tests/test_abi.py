@@ -93,3 +93,10 @@ def test_errors_raise_in_python():
     with pytest.raises(uhs.UhsError) as ei:
         uhs.validate(st, _grid(st, 0x10000), _grid(st, 0x20000))
     assert "multiple of 2" in str(ei.value)
+
+
+def test_wait_probe_rejects_bad_bounds_without_a_gpu():
+    """The failure probe validates its bound on the host, before any CUDA call."""
+    for cycles in (0, -5, (1 << 31) + 1):
+        assert uhs.probe_wait_timeout(cycles) == _lib.UHS_EINVAL
+        assert "cycles" in _lib.last_error()

@@ -82,6 +82,9 @@ struct MmaCall {
 };
 cudaError_t launch_box_mma(const MmaCall &c);
 
+// Failure-reporting probe (diag.cu): a bounded wait that cannot complete.
+cudaError_t launch_wait_probe(unsigned *err, long long cycles, cudaStream_t st);
+
 // Launch counter shared by every launcher.
 void count_launch(int n = 1);
 

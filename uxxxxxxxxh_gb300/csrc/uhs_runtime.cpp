@@ -1103,6 +1103,19 @@ void uhs_params_default(uhs_params *p) {
 
 int64_t uhs_launch_count(void) { return g_launches.load(); }
 
+int uhs_probe_wait_timeout(int64_t cycles, void *stream) {
+    if (cycles < 1 || cycles > (int64_t(1) << 31))
+        return set_error(UHS_EINVAL, "cycles must be in [1, 2^31] (got %lld)", static_cast<long long>(cycles));
+    int dev = 0;
+    cudaGetDevice(&dev);
+    unsigned *w = device_error_word(dev);
+    if (!w) return set_error(UHS_ENOMEM, "device status word allocation failed");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = launch_wait_probe(w, static_cast<long long>(cycles), st);
+    if (e != cudaSuccess) return cuda_error(e, "wait probe launch");
+    return finish(nullptr, st);
+}
+
 int uhs_error_norms(const uhs_stencil_desc *d, const uhs_memref *x, const uhs_memref *ref, double out[4],
                     void *stream) {
     int rc = validate_desc(d);

@@ -121,6 +121,13 @@ def launch_count() -> int:
     return int(_lib.lib().uhs_launch_count())
 
 
+def probe_wait_timeout(cycles: int, stream=None) -> int:
+    """Run the failure-reporting probe (uhs_probe_wait_timeout): a device wait
+    that runs out after `cycles` SM clocks.  Returns the status code (the
+    library reports UHS_ETIMEOUT); uhs_last_error() holds the message."""
+    return int(_lib.lib().uhs_probe_wait_timeout(int(cycles), _stream_handle(stream)))
+
+
 def error_norms(stencil: Stencil, x, ref, stream=None) -> dict:
     """FP64 error of device grid x against the FP64 device grid ref over the
     stencil's domain, reduced on the GPU (uhs_error_norms)."""
