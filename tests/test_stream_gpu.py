@@ -56,6 +56,28 @@ def test_stream_f32(cuda, rank, r, kind):
     assert oracle.halo_diff(st32, a32, ga) == 0
 
 
+@pytest.mark.parametrize("r", [1, 2, 3])
+def test_stream_f32_star_vy8(cuda, r):
+    """The FP32 star tile with 8 points per thread along y (32 x 4 threads),
+    ragged in y and x; the planner refuses it for other shapes and types."""
+    import torch
+    st, a0 = random_case(3, r, "star", (21, 45, 70), 6, 60 + r)
+    a32 = a0.astype(np.float32)
+    ra, _ = run_oracle(st, a32.astype(np.float64))
+    st32 = st.with_(dtype=uhs.UHS_F32)
+    p = uhs.RunParams(kernel=STREAM, tile_x=32, tile_y=32, vy=8)
+    assert uhs.plan(st32, params=p).vy == 8
+    ga, _ = run_gpu(st32, a32, p, dtype=torch.float32)
+    e = oracle.error(st, ra, ga)
+    assert e["l2_rel"] <= 1e-6, e
+    assert oracle.halo_diff(st32, a32, ga) == 0
+    with pytest.raises(uhs.UhsError):
+        uhs.plan(st, params=p)  # FP64
+    stb, _ = random_case(3, 1, "box", (8, 8, 32), 2, 63, dtype=uhs.UHS_F32)
+    with pytest.raises(uhs.UhsError):
+        uhs.plan(stb, params=p)
+
+
 def _pairs(a: np.ndarray) -> np.ndarray:
     hi = a.astype(np.float32)
     lo = (a - hi.astype(np.float64)).astype(np.float32)

@@ -81,6 +81,7 @@ struct TileShape {
 inline TileShape tile_shape(bool is2d, int tile) {
     if (is2d) return tile == 1 ? TileShape{64, 1, 1} : tile == 2 ? TileShape{256, 1, 1} : TileShape{128, 1, 1};
     switch (tile) {
+        case 4: return TileShape{32, 4, 8};
         case 1: return TileShape{32, 4, 4};
         case 2: return TileShape{64, 4, 2};
         case 3: return TileShape{32, 8, 2};

@@ -71,6 +71,11 @@ cudaError_t dispatch_tile(const StreamCall &c) {
             return launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 32, 8, 2, 2>>(c);
         } else {
             switch (c.tile) {
+                case 4:  // FP32 stars only: 8 points per thread along y
+                    if constexpr (ST == kStF32 && SHAPE == kStar3)
+                        return launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 32, 4, 8, PD>>(c);
+                    else
+                        return cudaErrorInvalidValue;
                 case 1: return launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 32, 4, 4, PD>>(c);
                 case 2: return launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 64, 4, 2, PD>>(c);
                 case 3: return launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 32, 8, 2, PD>>(c);

@@ -383,14 +383,23 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
         else if (cfg.tile_x != 0 && cfg.tile_x != 128)
             return set_error(UHS_EINVAL, "rank-2 streaming tiles are 64, 128 or 256 wide (got %d)", cfg.tile_x);
     } else if (cfg.tile_x == 0 && cfg.tile_y == 0 && p->vy == 0) {
-        // measured on GB300 (3d7pt, 512^3): df32 fastest at 64 x 8, native FP32 at 32 x 32
-        tile = arith == UHS_ARITH_DF32 ? 2 : 0;
+        // measured on GB300 (512^3): df32 fastest at 64 x 8; native FP32 at
+        // 32 x 32, with 8 points per thread for stars of radius 2-3 on grids
+        // of 256 rows or more (3d3r: 408 vs 340 GStencil/s at 4 points;
+        // fewer rows leave too few 32-row tiles)
+        const bool vy8 = sp.dtype == UHS_F32 && shape == kStar3 && R >= 2 && sp.ub[1] - sp.lb[1] >= 256;
+        tile = arith == UHS_ARITH_DF32 ? 2 : vy8 ? 4 : 0;
     } else {
         if (cfg.tile_x == 64) tile = 2;
         else if (cfg.tile_x != 0 && cfg.tile_x != 32)
             return set_error(UHS_EINVAL, "rank-3 streaming tiles are 32 or 64 wide (got %d)", cfg.tile_x);
         else if (cfg.tile_y == 16) tile = p->vy == 2 ? 3 : 1;
         else if (p->vy == 2) tile = 3;
+        else if (p->vy == 8) {
+            if (!(sp.dtype == UHS_F32 && shape == kStar3))
+                return set_error(UHS_EUNSUPPORTED, "8 points per thread along y: FP32 3D stars only");
+            tile = 4;
+        }
     }
     pl->tile = tile;
     // the kernel keeps in-plane offsets in 32 bits

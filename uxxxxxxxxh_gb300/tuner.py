@@ -11,12 +11,13 @@ tuner database (uhs_tune_put), which the planner consults whenever a caller
 leaves the parameters on auto.  Every timing is also kept as a training
 record for the learned cost model (costmodel.py).
 
-Candidates (rank 3): tile {32x32 VY4, 32x16 VY4, 64x8 VY2, 32x16 VY2} x
+Candidates (rank 3): tile {32x32 VY4, 32x16 VY4, 64x8 VY2, 32x16 VY2, and for
+FP32 stars 32x32 VY8} x
 loader {TMA, cp.async} x z-chunk {auto, 16, 64} x arithmetic (FP64:
 {float pairs, native}); rank 2: rows {64, 128, 256} x loader x z-chunk
-{auto, 128, 512} x arithmetic; plus the generic kernel, and for FP32 3D boxes
-of radius 2 and 3 the tensor-core kernel (16 or 32 columns).  Candidates that
-plan to the same launch are timed once.
+{auto, 128, 512} x arithmetic; plus the generic kernel, and on request
+(include_mma) for FP32 3D boxes of radius 2 and 3 the tensor-core kernel (16
+or 32 columns).  Candidates that plan to the same launch are timed once.
 """
 from __future__ import annotations
 
@@ -31,7 +32,7 @@ from .runtime import RunParams, memref_of, memref_raw, plan
 from .stencil import Stencil
 
 STREAM, GENERIC, MMA = _lib.UHS_KERNEL_STREAM, _lib.UHS_KERNEL_GENERIC, _lib.UHS_KERNEL_MMA
-TILES3 = [(32, 32, 4), (32, 16, 4), (64, 8, 2), (32, 16, 2)]
+TILES3 = [(32, 32, 4), (32, 16, 4), (64, 8, 2), (32, 16, 2), (32, 32, 8)]
 TILES2 = [64, 128, 256]
 
 
@@ -56,14 +57,14 @@ def config_features(p: RunParams, st: Stencil | None = None) -> list:
     """Launch features of a planned configuration: tile one-hot, loader,
     arithmetic, z-chunk, generic kernel, and (given the program) how the tile
     quantises its domain: log2 CTA tiles and the idle fraction of edge tiles."""
-    tile = [0.0] * 7
+    tile = [0.0] * (len(TILES3) + len(TILES2))
     if p.kernel == STREAM:
         if p.tile_y > 1:
             key = (p.tile_x, p.tile_y, p.vy)
             if key in TILES3:
                 tile[TILES3.index(key)] = 1.0
         elif p.tile_x in TILES2:
-            tile[4 + TILES2.index(p.tile_x)] = 1.0
+            tile[len(TILES3) + TILES2.index(p.tile_x)] = 1.0
     quant = [0.0, 0.0, 0.0]
     if st is not None and p.tile_x > 0:
         ext = [max(1, u - l) for l, u in zip(st.lb, st.ub)]
@@ -76,16 +77,18 @@ def config_features(p: RunParams, st: Stencil | None = None) -> list:
                    1.0 if p.kernel == MMA else 0.0] + quant
 
 
-N_FEATURES = 9 + 15
+N_FEATURES = 9 + 16
 
 
 def features(st: Stencil, p: RunParams, cls: list | None = None) -> list:
     return (cls if cls is not None else class_features(st)) + config_features(p, st)
 
 
-def candidates(st: Stencil) -> list:
+def candidates(st: Stencil, include_mma: bool = False) -> list:
     """Distinct planned launches to try for st (planned without the tuner
-    database so each candidate is what it says)."""
+    database so each candidate is what it says).  The tensor-core kernel is
+    left out unless include_mma: its error is an order of magnitude above the
+    CUDA-core FP32 sweep's, and a tuned entry is what UHS_KERNEL_AUTO runs."""
     out, seen = [], set()
     ariths = [_lib.UHS_ARITH_DF32, _lib.UHS_ARITH_FMA] if st.dtype == _lib.UHS_F64 else \
         ([_lib.UHS_ARITH_DF32] if st.dtype == _lib.UHS_F32X2 else [_lib.UHS_ARITH_FMA])
@@ -96,7 +99,7 @@ def candidates(st: Stencil) -> list:
            for ar in ariths for t in tiles for tma in (1, -1) for tz in zs]
     if st.dtype != _lib.UHS_F32X2:
         raw.append(RunParams(kernel=GENERIC, arith=_lib.UHS_ARITH_FMA, flags=_lib.UHS_FLAG_NO_TUNE_DB))
-    if st.dtype == _lib.UHS_F32 and st.rank == 3:
+    if include_mma and st.dtype == _lib.UHS_F32 and st.rank == 3:
         raw += [RunParams(kernel=MMA, tile_x=tx, flags=_lib.UHS_FLAG_NO_TUNE_DB) for tx in (16, 32)]
     # plan against the program's contiguous layout (a 256-byte aligned base,
     # as device allocations are) so loader eligibility is the grid's own
@@ -178,12 +181,12 @@ class Tuner:
         f = class_features(st)
         return f"r{st.rank}_R{round(f[1] * 3)}_{'box' if f[2] else 'star'}_{st.dtype}_{ext}"
 
-    def tune(self, st: Stencil, a=None, b=None, reps: int = 3, push: bool = True) -> tuple:
+    def tune(self, st: Stencil, a=None, b=None, reps: int = 3, push: bool = True, include_mma: bool = False) -> tuple:
         if a is None:
             a, b = device_grids(st)
         results = []
         cls = class_features(st)
-        for p in candidates(st):
+        for p in candidates(st, include_mma):
             try:
                 ns = measure(st, a, b, p, reps)
             except _lib.UhsError:
