@@ -247,6 +247,12 @@ int uhs_tune_put(const uhs_stencil_desc *desc, const uhs_params *best, double gs
 int uhs_tune_get(const uhs_stencil_desc *desc, uhs_params *out, int32_t *exact);
 void uhs_tune_clear(void);
 int64_t uhs_tune_size(void);
+/* Persist the database as text (written to path.tmp, then renamed) and merge
+ * a saved one back.  uhs_tune_load checks the whole file first: a file that
+ * does not parse, or holds a field out of range, returns UHS_EPARSE and
+ * changes nothing. */
+int uhs_tune_save(const char *path);
+int uhs_tune_load(const char *path);
 
 /* ---- learned cost model --------------------------------------------------- */
 /* A small MLP (in_dim -> hidden x layers (ReLU) -> 1) trained and evaluated by
@@ -280,6 +286,11 @@ int64_t uhs_launch_count(void);
  * faults and the device stays usable.  Returns UHS_ETIMEOUT with the message
  * the sweeps would give, after the stream drained. */
 int uhs_probe_wait_timeout(int64_t cycles, void *stream);
+
+/* Diagnostics: fail every library-owned device allocation larger than
+ * `bytes` as an out-of-memory would (0 removes the cap), so callers can test
+ * their handling of UHS_ENOMEM.  Allocations already made are kept. */
+int uhs_set_alloc_cap(int64_t bytes);
 
 #ifdef __cplusplus
 }

@@ -39,3 +39,31 @@ def test_timeout_on_a_stream_then_sweeps_on_it(cuda):
     ra, _ = run_oracle(st, a0)
     assert_f64_close(st, ra, a.cpu().numpy().reshape(-1))
     assert np.isfinite(a.cpu().numpy()).all()
+
+
+def test_allocation_failure_is_reported_and_recovers(cuda):
+    """A simulated out-of-memory (every library allocation above 64 bytes
+    fails): batch creation and the MLP report UHS_ENOMEM and leak nothing;
+    with the cap removed the same calls succeed."""
+    import torch
+    from uxxxxxxxxh_gb300.costmodel import MLP
+    L = _lib.lib()
+    st, a0 = random_case(3, 1, "star", (16, 16, 32), 2, 93)
+    a = torch.from_numpy(a0.reshape(st.sizes)).cuda()
+    b = a.clone()
+    assert L.uhs_set_alloc_cap(64) == _lib.UHS_OK
+    try:
+        with pytest.raises(uhs.UhsError) as ei:
+            uhs.Batch([st], [a], [b], uhs.RunParams())
+        assert ei.value.code == _lib.UHS_ENOMEM
+        with pytest.raises(uhs.UhsError) as ei:
+            MLP(8, 16, 2)
+        assert ei.value.code == _lib.UHS_ENOMEM
+    finally:
+        assert L.uhs_set_alloc_cap(0) == _lib.UHS_OK
+    batch = uhs.Batch([st], [a], [b], uhs.RunParams())
+    batch.run()
+    ra, _ = run_oracle(st, a0)
+    assert_f64_close(st, ra, a.cpu().numpy().reshape(-1))
+    assert MLP(8, 16, 2).num_params > 0
+    assert L.uhs_set_alloc_cap(-1) == _lib.UHS_EINVAL

@@ -69,6 +69,9 @@ SIGNATURES = {
     "uhs_plan": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Params), POINTER(Params)]),
     "uhs_launch_count": (c_int64, []),
     "uhs_probe_wait_timeout": (c_int, [c_int64, c_void_p]),
+    "uhs_set_alloc_cap": (c_int, [c_int64]),
+    "uhs_tune_save": (c_int, [c_char_p]),
+    "uhs_tune_load": (c_int, [c_char_p]),
     "uhs_mlp_create": (c_int, [c_int32, c_int32, c_int32, ctypes.c_uint64, POINTER(c_void_p)]),
     "uhs_mlp_destroy": (None, [c_void_p]),
     "uhs_mlp_num_params": (c_int64, [c_void_p]),

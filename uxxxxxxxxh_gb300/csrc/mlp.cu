@@ -141,10 +141,10 @@ cudaError_t reserve(uhs_mlp *m, int64_t rows) {
     m->act.assign(m->dims.size(), nullptr);
     m->dact.assign(m->dims.size(), nullptr);
     for (size_t l = 0; l < m->dims.size(); ++l) {
-        if (cudaMalloc(&m->act[l], sizeof(float) * rows * m->dims[l]) != cudaSuccess) return cudaErrorMemoryAllocation;
-        if (cudaMalloc(&m->dact[l], sizeof(float) * rows * m->dims[l]) != cudaSuccess) return cudaErrorMemoryAllocation;
+        if (dev_alloc((void **)&m->act[l], sizeof(float) * rows * m->dims[l]) != cudaSuccess) return cudaErrorMemoryAllocation;
+        if (dev_alloc((void **)&m->dact[l], sizeof(float) * rows * m->dims[l]) != cudaSuccess) return cudaErrorMemoryAllocation;
     }
-    if (cudaMalloc(&m->y, sizeof(float) * rows) != cudaSuccess) return cudaErrorMemoryAllocation;
+    if (dev_alloc((void **)&m->y, sizeof(float) * rows) != cudaSuccess) return cudaErrorMemoryAllocation;
     m->cap = rows;
     return cudaSuccess;
 }
@@ -182,6 +182,7 @@ void backward(uhs_mlp *m, int n) {
 }  // namespace
 }  // namespace uhs
 
+using uhs::dev_alloc;
 using uhs::set_error;
 
 extern "C" {
@@ -210,8 +211,8 @@ int uhs_mlp_create(int32_t in_dim, int32_t hidden, int32_t layers, uint64_t seed
         for (int64_t i = 0; i < static_cast<int64_t>(din) * dout; ++i) h[m->off[l] + i] = U(rng);
     }
     const size_t bytes = sizeof(float) * static_cast<size_t>(m->nparam);
-    if (cudaMalloc(&m->w, bytes) || cudaMalloc(&m->g, bytes) || cudaMalloc(&m->m, bytes) ||
-        cudaMalloc(&m->v, bytes) || cudaMalloc(&m->loss, sizeof(float))) {
+    if (dev_alloc((void **)&m->w, bytes) || dev_alloc((void **)&m->g, bytes) || dev_alloc((void **)&m->m, bytes) ||
+        dev_alloc((void **)&m->v, bytes) || dev_alloc((void **)&m->loss, sizeof(float))) {
         delete m;
         return set_error(UHS_ENOMEM, "MLP allocation failed");
     }
@@ -286,8 +287,8 @@ int uhs_mlp_train(uhs_mlp *m, const float *x, const float *y, int32_t n, int32_t
     batch = std::min(batch, n);
     float *dx = nullptr, *dy = nullptr;
     int *didx = nullptr;
-    if (cudaMalloc(&dx, sizeof(float) * n * m->in_dim) || cudaMalloc(&dy, sizeof(float) * n) ||
-        cudaMalloc(&didx, sizeof(int) * n)) {
+    if (dev_alloc((void **)&dx, sizeof(float) * n * m->in_dim) || dev_alloc((void **)&dy, sizeof(float) * n) ||
+        dev_alloc((void **)&didx, sizeof(int) * n)) {
         cudaFree(dx);
         cudaFree(dy);
         return set_error(UHS_ENOMEM, "training set upload");

@@ -85,6 +85,11 @@ cudaError_t launch_box_mma(const MmaCall &c);
 // Failure-reporting probe (diag.cu): a bounded wait that cannot complete.
 cudaError_t launch_wait_probe(unsigned *err, long long cycles, cudaStream_t st);
 
+// Library-owned device allocations go through dev_alloc, which honours the
+// diagnostic cap set by uhs_set_alloc_cap (a request above the cap fails as
+// an out-of-memory would).
+cudaError_t dev_alloc(void **p, size_t bytes);
+
 // Launch counter shared by every launcher.
 void count_launch(int n = 1);
 

@@ -33,6 +33,17 @@ namespace uhs {
 static std::atomic<int64_t> g_launches{0};
 void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+static std::atomic<int64_t> g_alloc_cap{0};  // 0: no cap
+
+cudaError_t dev_alloc(void **p, size_t bytes) {
+    const int64_t cap = g_alloc_cap.load(std::memory_order_relaxed);
+    if (cap > 0 && static_cast<int64_t>(bytes) > cap) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes);
+}
+
 static thread_local std::string t_err = "no error";
 
 int set_error(int code, const char *fmt, ...) {
@@ -60,7 +71,7 @@ unsigned *device_error_word(int device) {
         // word 0: kernel status flags; word 1: range-scan / halo-check result;
         // words 2-7: where the first bounded wait gave up (set, block x, block z,
         // plane, ring slot, phase)
-        if (cudaMalloc(&p, 8 * sizeof(unsigned)) != cudaSuccess) return nullptr;
+        if (dev_alloc(&p, 8 * sizeof(unsigned)) != cudaSuccess) return nullptr;
         cudaMemset(p, 0, 8 * sizeof(unsigned));
         words[device] = static_cast<unsigned *>(p);
     }
@@ -952,7 +963,7 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
     // Upload.
     if (n > 0) {
         void *p = nullptr;
-        if (cudaMalloc(&p, sizeof(BatchGrid) * static_cast<size_t>(n)) != cudaSuccess)
+        if (dev_alloc(&p, sizeof(BatchGrid) * static_cast<size_t>(n)) != cudaSuccess)
             return set_error(UHS_ENOMEM, "batch argument upload: allocation failed");
         B->d_grids = static_cast<BatchGrid *>(p);
         if (cudaMemcpy(B->d_grids, host.data(), sizeof(BatchGrid) * static_cast<size_t>(n), cudaMemcpyHostToDevice) !=
@@ -963,7 +974,7 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
     for (int p = 0; p < kNumPacks; ++p) {
         if (items[p].empty()) continue;
         void *q = nullptr;
-        if (cudaMalloc(&q, sizeof(int4) * items[p].size()) != cudaSuccess)
+        if (dev_alloc(&q, sizeof(int4) * items[p].size()) != cudaSuccess)
             return set_error(UHS_ENOMEM, "batch item list: allocation failed");
         B->d_items[p] = static_cast<int4 *>(q);
         if (cudaMemcpy(q, items[p].data(), sizeof(int4) * items[p].size(), cudaMemcpyHostToDevice) != cudaSuccess)
@@ -980,7 +991,7 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
     const size_t n_counters = static_cast<size_t>(steps) * kNumPacks;
     if (n_counters > 0) {
         void *q = nullptr;
-        if (cudaMalloc(&q, sizeof(int) * n_counters) != cudaSuccess)
+        if (dev_alloc(&q, sizeof(int) * n_counters) != cudaSuccess)
             return set_error(UHS_ENOMEM, "batch item counters: allocation failed");
         B->d_counters = static_cast<int *>(q);
     }
@@ -1165,7 +1176,7 @@ int uhs_error_norms(const uhs_stencil_desc *d, const uhs_memref *x, const uhs_me
         buf[dev] = nullptr;
         cap[dev] = 0;
         void *p = nullptr;
-        if (cudaMalloc(&p, need * sizeof(double)) != cudaSuccess)
+        if (dev_alloc(&p, need * sizeof(double)) != cudaSuccess)
             return set_error(UHS_ENOMEM, "scratch allocation of %lld doubles failed", (long long)need);
         buf[dev] = static_cast<double *>(p);
         cap[dev] = need;
@@ -1366,6 +1377,98 @@ int uhs_tune_get(const uhs_stencil_desc *d, uhs_params *out, int32_t *exact) {
     bool ex = false;
     if (!tune_lookup(d, out, &ex)) return set_error(UHS_EINVAL, "the tuner database has no entry for this class");
     if (exact) *exact = ex ? 1 : 0;
+    return UHS_OK;
+}
+
+// File format: a header line "uhs-tune 1", then one entry per line:
+//   rank shape R dtype ext0 ext1 ext2 kernel arith tile_x tile_y tile_z
+//   k_temporal use_tma flags vy prefetch gstencil_per_s
+int uhs_tune_save(const char *path) {
+    if (!path) return set_error(UHS_EINVAL, "path is NULL");
+    std::map<TuneKey, TuneEntry> snap;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        snap = g_tune;
+    }
+    const std::string tmp = std::string(path) + ".tmp";
+    FILE *f = std::fopen(tmp.c_str(), "w");
+    if (!f) return set_error(UHS_EINVAL, "cannot write %s", tmp.c_str());
+    bool ok = std::fprintf(f, "uhs-tune 1\n") > 0;
+    for (const auto &kv : snap) {
+        const TuneKey &k = kv.first;
+        const uhs_params &q = kv.second.p;
+        ok = ok && std::fprintf(f, "%d %d %d %d %lld %lld %lld %d %d %d %d %d %d %d %d %d %d %.9g\n", k.rank, k.shape,
+                                k.R, k.dtype, static_cast<long long>(k.ext[0]), static_cast<long long>(k.ext[1]),
+                                static_cast<long long>(k.ext[2]), q.kernel, q.arith, q.tile_x, q.tile_y, q.tile_z,
+                                q.k_temporal, q.use_tma, q.flags, q.vy, q.prefetch, kv.second.gst) > 0;
+    }
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok || std::rename(tmp.c_str(), path) != 0) {
+        std::remove(tmp.c_str());
+        return set_error(UHS_EINVAL, "writing %s failed", path);
+    }
+    return UHS_OK;
+}
+
+// Entries are read into a scratch table and merged only when the whole file
+// parses and every field is in range: a truncated or corrupted file changes
+// nothing.
+int uhs_tune_load(const char *path) {
+    if (!path) return set_error(UHS_EINVAL, "path is NULL");
+    FILE *f = std::fopen(path, "r");
+    if (!f) return set_error(UHS_EINVAL, "cannot read %s", path);
+    std::map<TuneKey, TuneEntry> got;
+    char line[512];
+    int lineno = 0;
+    int rc = UHS_OK;
+    while (std::fgets(line, sizeof line, f)) {
+        ++lineno;
+        if (lineno == 1) {
+            if (std::strncmp(line, "uhs-tune 1", 10) != 0) {
+                rc = set_error(UHS_EPARSE, "%s: not a tuner database (header)", path);
+                break;
+            }
+            continue;
+        }
+        if (line[0] == '\n' || line[0] == '\0') continue;
+        TuneKey k{};
+        uhs_params q;
+        uhs_params_default(&q);
+        long long e0, e1, e2;
+        double gst = 0.0;
+        char extra[2];
+        const int n = std::sscanf(line, "%d %d %d %d %lld %lld %lld %d %d %d %d %d %d %d %d %d %d %lf %1s", &k.rank,
+                                  &k.shape, &k.R, &k.dtype, &e0, &e1, &e2, &q.kernel, &q.arith, &q.tile_x, &q.tile_y,
+                                  &q.tile_z, &q.k_temporal, &q.use_tma, &q.flags, &q.vy, &q.prefetch, &gst, extra);
+        k.ext[0] = e0;
+        k.ext[1] = e1;
+        k.ext[2] = e2;
+        const bool shape_ok = k.rank == 3 ? (k.shape == kStar3 || k.shape == kBox3)
+                                          : (k.rank == 2 && (k.shape == kStar2 || k.shape == kBox2));
+        const bool in_range = n == 18 && shape_ok &&
+                              k.R >= 1 && k.R <= 3 && k.dtype >= UHS_F64 && k.dtype <= UHS_F32X2 && e0 >= 1 &&
+                              e1 >= 1 && e2 >= 1 && q.kernel >= UHS_KERNEL_AUTO && q.kernel <= UHS_KERNEL_MMA &&
+                              q.arith >= UHS_ARITH_AUTO && q.arith <= UHS_ARITH_DF32 && q.tile_x >= 0 &&
+                              q.tile_x <= 1024 && q.tile_y >= 0 && q.tile_y <= 1024 && q.tile_z >= 0 &&
+                              q.k_temporal >= 0 && q.k_temporal <= 4 && q.use_tma >= -1 && q.use_tma <= 1 &&
+                              q.vy >= 0 && q.vy <= 8 && q.prefetch >= 0 && q.prefetch <= 8 && std::isfinite(gst);
+        if (!in_range) {
+            rc = set_error(UHS_EPARSE, "%s:%d: malformed tuner entry", path, lineno);
+            break;
+        }
+        got[k] = TuneEntry{q, gst};
+    }
+    if (rc == UHS_OK && lineno == 0) rc = set_error(UHS_EPARSE, "%s: empty file", path);
+    std::fclose(f);
+    if (rc != UHS_OK) return rc;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (const auto &kv : got) g_tune[kv.first] = kv.second;
+    return UHS_OK;
+}
+
+int uhs_set_alloc_cap(int64_t bytes) {
+    if (bytes < 0) return set_error(UHS_EINVAL, "the cap must be >= 0 (0: none)");
+    g_alloc_cap.store(bytes);
     return UHS_OK;
 }
 

@@ -229,3 +229,14 @@ def db_get(st: Stencil):
 
 def db_clear() -> None:
     _lib.lib().uhs_tune_clear()
+
+
+def db_save(path: str) -> None:
+    """Write the library's tuner database to path (uhs_tune_save)."""
+    _lib.check(_lib.lib().uhs_tune_save(os.fsencode(path)))
+
+
+def db_load(path: str) -> None:
+    """Merge a saved tuner database into the library's (uhs_tune_load); a
+    malformed file raises UhsError(UHS_EPARSE) and changes nothing."""
+    _lib.check(_lib.lib().uhs_tune_load(os.fsencode(path)))
