@@ -291,7 +291,10 @@ def bench_batch(args, rank: int, world: int, local: int):
     import torch
     import uxxxxxxxxh_gb300 as uhs
     from uxxxxxxxxh_gb300.workloads import cfg5_specs
-    specs = cfg5_specs(n_grids=64, T=args.iters or 20)
+    # --side N: the same suite drawn on smaller grids (3D sides up to N, 2D up
+    # to 8N), for profiling runs
+    specs = cfg5_specs(n_grids=64, T=args.iters or 20) if not args.side else \
+        cfg5_specs(n_grids=64, T=args.iters or 20, side2=(64, 8 * args.side), side3=(16, args.side))
     gen = torch.Generator(device="cuda")
     A, B = [], []
     for st, seed in specs:
@@ -330,9 +333,10 @@ def bench_batch(args, rank: int, world: int, local: int):
     line = {"metric": "GStencil/s", "value": value, "unit": "GStencil/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)",
-            "config": {"workload": "cfg5 batched mixed suite: 64 grids, 12 shapes, FP32+FP64, T=20",
+            "config": {"workload": "cfg5 batched mixed suite: 64 grids, 12 shapes, FP32+FP64, "
+                                   f"T={specs[0][0].iterations}" + (f", 3D sides <= {args.side}" if args.side else ""),
                        "launches_per_step": st_["launches"], "timesteps": st_["steps"],
-                       "work_items_per_timestep": st_["items"], "l2": "5.4 GB of grids, larger than L2"},
+                       "work_items_per_timestep": st_["items"], "l2": f"{sum(2 * st.elem_bytes * st.sizes[0] * st.sizes[1] * st.sizes[2] for st, _ in specs) / 1e9:.1f} GB of grids"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_source": peak_kind},
             "gpu_launches": uhs.launch_count() - n0, "clocks": clk}
