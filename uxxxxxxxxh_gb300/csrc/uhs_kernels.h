@@ -41,7 +41,7 @@ struct LaunchCfg {
 // Device-side error word written by kernels that detect a problem (range
 // overflow in float-pair arithmetic, a bounded wait that ran out).
 enum : unsigned { kDevErrRange = 1u, kDevErrTimeout = 2u };
-unsigned *device_error_word(int device);
+unsigned *stream_error_word(int device, cudaStream_t stream);
 
 // Generic smem plane-ring sweep: any term list, expression order.
 cudaError_t launch_generic(const SweepSpec &sp, const LaunchCfg &cfg, const GridView &in,

@@ -61,21 +61,29 @@ static int cuda_error(cudaError_t e, const char *what) {
 }
 
 // Per-device error word (see uhs_kernels.h).  Allocated on first use.
-unsigned *device_error_word(int device) {
+// Status words (8 x unsigned) in device memory, one per (device, stream),
+// allocated at first use and kept for the process:
+//   word 0: kernel status flags; word 1: range-scan / halo-check result;
+//   words 2-7: where the first bounded wait gave up (set, block x, block z,
+//   plane, ring slot, phase).
+// Calls on different streams (or host threads with their own streams) never
+// share a word, so one call's errors and scan results cannot leak into
+// another's.
+unsigned *stream_error_word(int device, cudaStream_t stream) {
     static std::mutex mu;
-    static unsigned *words[64] = {};
-    if (device < 0 || device >= 64) return nullptr;
+    static std::map<std::pair<int, uintptr_t>, unsigned *> words;
+    const auto key = std::make_pair(device, reinterpret_cast<uintptr_t>(stream));
     std::lock_guard<std::mutex> lk(mu);
-    if (!words[device]) {
-        void *p = nullptr;
-        // word 0: kernel status flags; word 1: range-scan / halo-check result;
-        // words 2-7: where the first bounded wait gave up (set, block x, block z,
-        // plane, ring slot, phase)
-        if (dev_alloc(&p, 8 * sizeof(unsigned)) != cudaSuccess) return nullptr;
-        cudaMemset(p, 0, 8 * sizeof(unsigned));
-        words[device] = static_cast<unsigned *>(p);
+    auto it = words.find(key);
+    if (it != words.end()) return it->second;
+    void *p = nullptr;
+    if (dev_alloc(&p, 8 * sizeof(unsigned)) != cudaSuccess) return nullptr;
+    if (cudaMemset(p, 0, 8 * sizeof(unsigned)) != cudaSuccess) {
+        cudaFree(p);
+        return nullptr;
     }
-    return words[device];
+    words[key] = static_cast<unsigned *>(p);
+    return static_cast<unsigned *>(p);
 }
 
 static size_t elem_bytes(int dtype) { return dtype == UHS_F32 ? 4 : 8; }
@@ -525,7 +533,7 @@ static GridView kernel_view(const SweepSpec &sp, const GridView &v) {
 static bool range_ok(const SweepSpec &sp, const GridView &a, const GridView &b, int T, cudaStream_t st) {
     int dev = 0;
     cudaGetDevice(&dev);
-    unsigned *w = device_error_word(dev);
+    unsigned *w = stream_error_word(dev, st);
     if (!w) return false;
     unsigned *scan = w + 1;
     if (cudaMemsetAsync(scan, 0, sizeof(unsigned), st) != cudaSuccess) return false;
@@ -565,7 +573,7 @@ static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in,
         m.stream = st;
         int dev = 0;
         cudaGetDevice(&dev);
-        m.err = device_error_word(dev);
+        m.err = stream_error_word(dev, st);
         if (!m.err) return set_error(UHS_ENOMEM, "device error word allocation failed");
         cudaError_t e = launch_box_mma(m);
         if (e != cudaSuccess) return cuda_error(e, "tensor-core box sweep launch");
@@ -591,7 +599,7 @@ static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in,
     c.stream = st;
     int dev = 0;
     cudaGetDevice(&dev);
-    c.err = device_error_word(dev);
+    c.err = stream_error_word(dev, st);
     if (!c.err) return set_error(UHS_ENOMEM, "device error word allocation failed");
     const int eb = sp.dtype == UHS_F32 ? 4 : 8;
     CUtensorMap tmap;
@@ -665,7 +673,7 @@ static std::vector<int> plan_passes(int T, int k) {
 static int halos_equal(const SweepSpec &sp, const GridView &a, const GridView &b, cudaStream_t st, bool *eq) {
     int dev = 0;
     cudaGetDevice(&dev);
-    unsigned *w = device_error_word(dev);
+    unsigned *w = stream_error_word(dev, st);
     if (!w) return set_error(UHS_ENOMEM, "device status word allocation failed");
     unsigned *cnt = w + 1;
     cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(unsigned), st);
@@ -696,7 +704,8 @@ static int launch_fused_pass(const SweepSpec &sp, const Plan &pl, const GridView
     c.stream = st;
     int dev = 0;
     cudaGetDevice(&dev);
-    c.err = device_error_word(dev);
+    c.err = stream_error_word(dev, st);
+    if (!c.err) return set_error(UHS_ENOMEM, "device error word allocation failed");
     const int64_t nz = sp.ub[0] - sp.lb[0];
     const int64_t tiles = ((sp.ub[2] - sp.lb[2] + 31) / 32) * ((sp.ub[1] - sp.lb[1] + 15) / 16);
     int zchunk = pl.cfg.tile_z;
@@ -716,10 +725,7 @@ static int launch_fused_pass(const SweepSpec &sp, const Plan &pl, const GridView
 }
 
 // Read and clear the device error word after the stream drained.
-static int check_device_errors(cudaStream_t st) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    unsigned *w = device_error_word(dev);
+static int check_status_word(unsigned *w, cudaStream_t st) {
     if (!w) return UHS_OK;
     unsigned h[8] = {};
     cudaError_t e = cudaMemcpyAsync(h, w, sizeof h, cudaMemcpyDeviceToHost, st);
@@ -735,6 +741,12 @@ static int check_device_errors(cudaStream_t st) {
                          h[3], h[4], h[5], h[6], h[7]);
     return set_error(UHS_ERANGE, "a grid value is outside the float-pair range [2^-126, 2^128); "
                                  "run this grid with UHS_ARITH_FMA");
+}
+
+static int check_device_errors(cudaStream_t st) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return check_status_word(stream_error_word(dev, st), st);
 }
 
 static int finish(const uhs_params *p, cudaStream_t st) {
@@ -821,6 +833,7 @@ struct uhs_batch_impl {
     BatchGrid *d_grids = nullptr;
     int4 *d_items[kNumPacks] = {nullptr, nullptr};
     int *d_counters = nullptr;  // one item counter per (timestep, pack), zeroed at each replay
+    unsigned *d_status = nullptr;  // the batch's own status word (its graph may replay on any stream)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -831,6 +844,7 @@ static void batch_free(uhs_batch_impl *b) {
     if (b->graph) cudaGraphDestroy(b->graph);
     if (b->d_grids) cudaFree(b->d_grids);
     if (b->d_counters) cudaFree(b->d_counters);
+    if (b->d_status) cudaFree(b->d_status);
     for (auto *p : b->d_items)
         if (p) cudaFree(p);
     delete b;
@@ -846,8 +860,13 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
     std::vector<BatchGrid> host(static_cast<size_t>(n));
     std::vector<BatchGridHost> info(static_cast<size_t>(n));
     std::vector<std::vector<int4>> items(kNumPacks);
-    unsigned *err = device_error_word(B->dev);
-    if (!err) return set_error(UHS_ENOMEM, "device status word allocation failed");
+    {
+        void *q = nullptr;
+        if (dev_alloc(&q, 8 * sizeof(unsigned)) != cudaSuccess || cudaMemset(q, 0, 8 * sizeof(unsigned)) != cudaSuccess)
+            return set_error(UHS_ENOMEM, "batch status word allocation failed");
+        B->d_status = static_cast<unsigned *>(q);
+    }
+    unsigned *err = B->d_status;
     cudaStream_t scan_stream = nullptr;
     if (cudaStreamCreateWithFlags(&scan_stream, cudaStreamNonBlocking) != cudaSuccess)
         return set_error(UHS_ECUDA, "stream creation failed");
@@ -1131,9 +1150,9 @@ int uhs_probe_wait_timeout(int64_t cycles, void *stream) {
         return set_error(UHS_EINVAL, "cycles must be in [1, 2^31] (got %lld)", static_cast<long long>(cycles));
     int dev = 0;
     cudaGetDevice(&dev);
-    unsigned *w = device_error_word(dev);
-    if (!w) return set_error(UHS_ENOMEM, "device status word allocation failed");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    unsigned *w = stream_error_word(dev, st);
+    if (!w) return set_error(UHS_ENOMEM, "device status word allocation failed");
     cudaError_t e = launch_wait_probe(w, static_cast<long long>(cycles), st);
     if (e != cudaSuccess) return cuda_error(e, "wait probe launch");
     return finish(nullptr, st);
@@ -1332,10 +1351,10 @@ int uhs_batch_run(uhs_batch *batch, void *stream, int32_t flags) {
         if (e != cudaSuccess) return cuda_error(e, "batch graph launch");
         count_launch(static_cast<int>(batch->impl->launches));
     }
-    uhs_params p;
-    uhs_params_default(&p);
-    p.flags = flags;
-    return finish(&p, st);
+    if (flags & UHS_FLAG_NO_SYNC) return UHS_OK;
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(e, "stream synchronise");
+    return check_status_word(batch->impl->d_status, st);
 }
 
 int uhs_batch_stats(const uhs_batch *batch, int64_t *launches, int64_t *steps, int64_t *items) {
