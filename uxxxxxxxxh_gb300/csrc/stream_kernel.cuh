@@ -546,12 +546,9 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
     return true;
 }
 
-// FP32 variants of 256 threads are held to 64 registers (4 CTAs per SM, half
-// the warp slots instead of 3/8 at the 72 registers they would take): no
-// spills, and on GB300 2-3 % faster (cfg2 FP32 584 vs 573 GStencil/s).
+// One CTA's work: mbarrier set-up for the TMA loader, then the item.
 template <class C>
-__global__ void __launch_bounds__(C::THREADS, (C::ST == kStF32 && C::THREADS == 256 ? 4 : 1))
-    k_stream(const __grid_constant__ StreamArgs<C::NT> a) {
+__device__ __forceinline__ void stream_cta(const StreamArgs<C::NT> &a) {
     extern __shared__ __align__(128) unsigned char smem[];
     if constexpr (C::LD == kLdTma) {
         uint64_t *const mbar = reinterpret_cast<uint64_t *>(smem + C::NSTG * C::STG_SLOT +
@@ -563,6 +560,28 @@ __global__ void __launch_bounds__(C::THREADS, (C::ST == kStF32 && C::THREADS == 
         __syncthreads();
     }
     (void)stream_item<C>(a, blockIdx.x, blockIdx.y, blockIdx.z, smem);
+}
+
+template <class C>
+__global__ void __launch_bounds__(C::THREADS) k_stream(const __grid_constant__ StreamArgs<C::NT> a) {
+    stream_cta<C>(a);
+}
+
+// FP32 variants run as k_stream_occ4, held to 4 CTAs per SM: the 256-thread
+// tiles to 64 registers (half the warp slots instead of 3/8 at the 72 they
+// would take; no spills, 2-3 % faster on GB300, cfg2 FP32 584 vs 573
+// GStencil/s) and the 128-thread VY 8 tiles to 128 (3d3r FP32 star 421 vs 305
+// GStencil/s at the 185 registers and 2 CTAs they would take).  The other
+// variants keep ptxas's own register choice: the float-pair 3d7pt kernel
+// takes 32 registers there and 47 under an explicit minimum of one CTA,
+// which costs it 10 %.
+template <class C>
+constexpr bool stream_occ4() {
+    return C::ST == kStF32 && (C::THREADS == 256 || C::VY == 8);
+}
+template <class C>
+__global__ void __launch_bounds__(C::THREADS, 4) k_stream_occ4(const __grid_constant__ StreamArgs<C::NT> a) {
+    stream_cta<C>(a);
 }
 
 }  // namespace uhs

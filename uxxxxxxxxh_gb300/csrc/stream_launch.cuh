@@ -36,18 +36,21 @@ cudaError_t launch_cfg(const StreamCall &c) {
     fill_coefs(a.cd, a.chl, a.cl_sum, c.coef, C::NT, c.shape, c.R);
     const int64_t nz = c.ub[0] - c.lb[0], ny = c.ub[1] - c.lb[1], nx = c.ub[2] - c.lb[2];
     if (!c.occ_out && (nz <= 0 || ny <= 0 || nx <= 0)) return cudaSuccess;
+    void (*kern)(const StreamArgs<C::NT>);
+    if constexpr (stream_occ4<C>()) kern = k_stream_occ4<C>;
+    else kern = k_stream<C>;
     static bool attr_set = false;
     if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_stream<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
     if (c.occ_out) {
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(c.occ_out, k_stream<C>, C::THREADS, C::SMEM);
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(c.occ_out, kern, C::THREADS, C::SMEM);
     }
     dim3 grid(static_cast<unsigned>((nx + C::BX - 1) / C::BX), static_cast<unsigned>((ny + C::BY - 1) / C::BY),
               static_cast<unsigned>((nz + c.zchunk - 1) / c.zchunk));
-    k_stream<C><<<grid, dim3(C::BX, C::TYT), C::SMEM, c.stream>>>(a);
+    kern<<<grid, dim3(C::BX, C::TYT), C::SMEM, c.stream>>>(a);
     count_launch();
     return cudaGetLastError();
 }
