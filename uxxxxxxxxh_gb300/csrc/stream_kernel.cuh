@@ -286,48 +286,82 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
 
     // cp.async: per-thread row offsets inside a plane (32-bit: a plane holds
     // fewer than 2^31 elements, which the host checks) and validity.
-    int row_off[NLOAD_ROWS];
+    // 8-byte elements recompute each copy's source per plane (fewest live
+    // registers: these variants run at the compiler's register choice).
+    // 4-byte elements (FP32, held to 64 or 128 registers) hoist it: each
+    // copy's in-plane offset (0 when zero-filled) and a validity bit are
+    // computed once per z-chunk and only the plane pointer moves -- 2-4 %
+    // faster on GB300.
+    constexpr bool HOIST = C::EB == 4;
+    int row_off[NLOAD_ROWS];  // 8-byte elements
     bool row_ok[NLOAD_ROWS];
-#pragma unroll
-    for (int i = 0; i < NLOAD_ROWS; ++i) {
-        const int r = ty + i * TYT;
-        const int64_t gy = gy0 + r;
-        row_ok[i] = r < H && gy >= 0 && gy < a.n1;
-        row_off[i] = row_ok[i] ? static_cast<int>(gy * a.in_s1) : 0;
-    }
+    int off_a[NLOAD_ROWS], off_b[NLOAD_ROWS];  // 4-byte elements
+    unsigned ok_a = 0u, ok_b = 0u;
+    const bool pairs = C::EB == 4 && a.pair_loads;  // 8-byte granules, columns 2tx, 2tx+1
+    constexpr int NPAIR = (BX + 2 * R + 1) / 2;
     const int gxa = static_cast<int>(gx0) + tx, gxb = gxa + BX;
     const bool col_a = gxa >= 0 && gxa < a.n2;
     const bool col_b = tx < 2 * R && gxb < a.n2;
+    if constexpr (HOIST) {
+        const int gx1 = pairs ? static_cast<int>(gx0) + 2 * tx : gxa;
+        const bool c1 = pairs ? (tx < NPAIR && gx1 + 1 < a.n2) : col_a;
+        const bool c2 = !pairs && col_b;
+#pragma unroll
+        for (int i = 0; i < NLOAD_ROWS; ++i) {
+            const int r = ty + i * TYT;
+            const int64_t gy = gy0 + r;
+            const bool row = r < H && gy >= 0 && gy < a.n1;
+            const int ro = row ? static_cast<int>(gy * a.in_s1) : 0;
+            off_a[i] = row && c1 ? ro + gx1 : 0;
+            off_b[i] = row && c2 ? ro + gxb : 0;
+            ok_a |= static_cast<unsigned>(row && c1) << i;
+            ok_b |= static_cast<unsigned>(row && c2) << i;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < NLOAD_ROWS; ++i) {
+            const int r = ty + i * TYT;
+            const int64_t gy = gy0 + r;
+            row_ok[i] = r < H && gy >= 0 && gy < a.n1;
+            row_off[i] = row_ok[i] ? static_cast<int>(gy * a.in_s1) : 0;
+        }
+    }
+    const TS *plane_src = static_cast<const TS *>(a.in) + qbeg * a.in_s0;  // plane of the next issue
 
     auto issue = [&](int j, int slot) {
         const int64_t p = qbeg + j;
-        if constexpr (C::LD == kLdCpAsync) {
-            const TS *plane = static_cast<const TS *>(a.in) + p * a.in_s0;
+        if constexpr (C::LD == kLdCpAsync && HOIST) {
+            const TS *plane = plane_src;  // planes are issued in order, one each
+            plane_src += a.in_s0;
             TS *dst = stg_base + slot * STG_ELEMS;
-            if (C::EB == 4 && a.pair_loads) {
-                // 8-byte granules: thread tx copies columns 2tx, 2tx+1 (W is even).
-                constexpr int NPAIR = (BX + 2 * R + 1) / 2;
-                const int gxp = static_cast<int>(gx0) + 2 * tx;
-                const bool pok = tx < NPAIR && gxp + 1 < a.n2;
+            if (pairs) {
 #pragma unroll
                 for (int i = 0; i < NLOAD_ROWS; ++i) {
                     const int r = ty + i * TYT;
-                    if (r < H && tx < NPAIR) {
-                        const bool ok = row_ok[i] && pok;
-                        cp_async<8>(dst + r * W + 2 * tx, ok ? plane + row_off[i] + gxp : plane, ok);
-                    }
+                    if (r < H && tx < NPAIR) cp_async<8>(dst + r * W + 2 * tx, plane + off_a[i], (ok_a >> i) & 1u);
                 }
             } else {
 #pragma unroll
                 for (int i = 0; i < NLOAD_ROWS; ++i) {
                     const int r = ty + i * TYT;
                     if (r < H) {
-                        const TS *src = plane + row_off[i];
-                        cp_async<C::EB>(dst + r * W + tx, row_ok[i] && col_a ? src + gxa : plane, row_ok[i] && col_a);
-                        if (tx < 2 * R)
-                            cp_async<C::EB>(dst + r * W + tx + BX, row_ok[i] && col_b ? src + gxb : plane,
-                                            row_ok[i] && col_b);
+                        cp_async<C::EB>(dst + r * W + tx, plane + off_a[i], (ok_a >> i) & 1u);
+                        if (tx < 2 * R) cp_async<C::EB>(dst + r * W + tx + BX, plane + off_b[i], (ok_b >> i) & 1u);
                     }
+                }
+            }
+        } else if constexpr (C::LD == kLdCpAsync) {
+            const TS *plane = static_cast<const TS *>(a.in) + p * a.in_s0;
+            TS *dst = stg_base + slot * STG_ELEMS;
+#pragma unroll
+            for (int i = 0; i < NLOAD_ROWS; ++i) {
+                const int r = ty + i * TYT;
+                if (r < H) {
+                    const TS *src = plane + row_off[i];
+                    cp_async<C::EB>(dst + r * W + tx, row_ok[i] && col_a ? src + gxa : plane, row_ok[i] && col_a);
+                    if (tx < 2 * R)
+                        cp_async<C::EB>(dst + r * W + tx + BX, row_ok[i] && col_b ? src + gxb : plane,
+                                        row_ok[i] && col_b);
                 }
             }
         } else {
