@@ -100,3 +100,25 @@ def test_wait_probe_rejects_bad_bounds_without_a_gpu():
     for cycles in (0, -5, (1 << 31) + 1):
         assert uhs.probe_wait_timeout(cycles) == _lib.UHS_EINVAL
         assert "cycles" in _lib.last_error()
+
+
+def test_short_or_one_sided_reach_runs_on_the_generic_kernel():
+    """The templated star/box kernels read every cell within R on every axis;
+    a program reaching less (no z offsets, or only one side) must be planned
+    on the generic kernel, which reads only what the program reads."""
+    from uxxxxxxxxh_gb300.stencil import Stencil
+    # 3D, in-plane 5-point star, no z halo at all
+    st = Stencil(name="inplane", rank=3, sizes=(4, 10, 12), lb=(0, 1, 1), ub=(4, 9, 11),
+                 terms=[(0, -1, 0, 0.2), (0, 0, -1, 0.2), (0, 0, 0, 0.2), (0, 0, 1, 0.2), (0, 1, 0, 0.2)],
+                 iterations=2)
+    assert uhs.plan(st).kernel == uhs.UHS_KERNEL_GENERIC
+    with pytest.raises(uhs.UhsError):
+        uhs.plan(st, params=uhs.RunParams(kernel=uhs.UHS_KERNEL_STREAM))
+    # one-sided z reach (dz in {-1, 0}), halo only below
+    st2 = Stencil(name="upwind", rank=3, sizes=(6, 10, 12), lb=(1, 1, 1), ub=(6, 9, 11),
+                  terms=[(-1, 0, 0, 0.25), (0, -1, 0, 0.125), (0, 0, -1, 0.125), (0, 0, 0, 0.25), (0, 0, 1, 0.125),
+                         (0, 1, 0, 0.125)], iterations=2)
+    assert uhs.plan(st2).kernel == uhs.UHS_KERNEL_GENERIC
+    # a full star still plans on the streaming kernel
+    st3 = st2.with_(terms=st2.terms + [(1, 0, 0, 0.0)], ub=(5, 9, 11))
+    assert uhs.plan(st3).kernel == uhs.UHS_KERNEL_STREAM

@@ -83,8 +83,12 @@ __global__ void __launch_bounds__(256) k_generic(const __grid_constant__ Generic
     const int64_t ze = min(zs + (int64_t)a.zchunk, a.ub0);
     const int plane_elems = a.W * a.H;
 
+    // Ring slot of plane p.  Planes below 0 occur when the program reaches
+    // only upwards in z from a domain starting at 0; they are zero-filled
+    // and must still land in a slot of the ring, so the modulo is floored.
+    auto slot_of = [&](int64_t p) { return static_cast<int>(((p % a.NS) + a.NS) % a.NS); };
     auto load_plane = [&](int64_t p) {
-        T *dst = ring + (int)(p % a.NS) * plane_elems;
+        T *dst = ring + slot_of(p) * plane_elems;
         const bool zin = (p >= 0) && (p < a.n0);
         for (int r = ty; r < a.H; r += TY) {
             const int64_t gy = y0 - a.ry + r;
@@ -113,7 +117,7 @@ __global__ void __launch_bounds__(256) k_generic(const __grid_constant__ Generic
 
     for (int64_t z = zs; z < ze; ++z) {
         cp_async_wait_1();
-        if (ty == 0 && tx <= 2 * a.rz) plane_base[tx] = (int)((z - a.rz + tx) % a.NS) * plane_elems;
+        if (ty == 0 && tx <= 2 * a.rz) plane_base[tx] = slot_of(z - a.rz + tx) * plane_elems;
         __syncthreads();
         if (active) {
             const T *c0 = ring + center;

@@ -249,15 +249,29 @@ static int nterms_of(int shape, int R) {
 
 // Star if every offset lies on an axis, box otherwise; radius 1..3.  Rank-2
 // programs are streamed along y, so (dy, dx) become the kernel's (dz, dx).
+// Star or box of radius R for the templated kernels.  Those kernels read
+// every cell within R of the domain on every axis of the rank, so the
+// program must reach exactly -R..+R on each of them: a one-sided or shorter
+// reach on some axis (which check_reach would accept with a thinner halo)
+// would send them outside the grid, or into cells the program never reads.
+// Such programs run on the generic kernel.
 static bool classify(const SweepSpec &sp, int *shape, int *R) {
     int r = 0;
     bool on_axes = true;
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
     for (int k = 0; k < sp.nterms; ++k) {
-        const int a[3] = {std::abs(sp.dz[k]), std::abs(sp.dy[k]), std::abs(sp.dx[k])};
+        const int o[3] = {sp.dz[k], sp.dy[k], sp.dx[k]};
+        const int a[3] = {std::abs(o[0]), std::abs(o[1]), std::abs(o[2])};
         r = std::max({r, a[0], a[1], a[2]});
         if ((a[0] != 0) + (a[1] != 0) + (a[2] != 0) > 1) on_axes = false;
+        for (int i = 0; i < 3; ++i) {
+            lo[i] = std::min(lo[i], o[i]);
+            hi[i] = std::max(hi[i], o[i]);
+        }
     }
     if (r < 1 || r > 3) return false;
+    for (int i = (sp.rank == 3 ? 0 : 1); i < 3; ++i)
+        if (lo[i] != -r || hi[i] != r) return false;
     *R = r;
     if (sp.rank == 3) *shape = on_axes ? kStar3 : kBox3;
     else *shape = on_axes ? kStar2 : kBox2;
