@@ -86,6 +86,11 @@ def test_validate_rejects_bad_memrefs():
     b = _grid(st, 0x20004)
     assert _validate(st, a, b) == _lib.UHS_EINVAL                           # misaligned doubles
     assert _validate(st, a, uhs.memref_raw(0, st.sizes)) == _lib.UHS_EINVAL  # NULL
+    span = 8 * st.sizes[0] * st.sizes[1] * st.sizes[2]
+    assert _validate(st, a, _grid(st, 0x10000 + span)) == _lib.UHS_OK        # adjacent: fine
+    assert _validate(st, a, _grid(st, 0x10000 + span - 8)) == _lib.UHS_EINVAL  # last cell shared
+    assert "overlap" in _lib.last_error()
+    assert _validate(st, _grid(st, 0x10000 + span - 8), a) == _lib.UHS_EINVAL
 
 
 def test_errors_raise_in_python():

@@ -781,6 +781,18 @@ static int prepare(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_mem
             return set_error(UHS_EINVAL, "a and b differ in sizes[%d] (%lld vs %lld)", i, (long long)va->n[i],
                              (long long)vb->n[i]);
     if (va->data == vb->data) return set_error(UHS_EINVAL, "a and b are the same grid");
+    // The sweeps read one grid while writing the other: their address spans
+    // must not intersect (a grid's span runs from its first to its last cell).
+    {
+        const auto span_end = [&](const GridView &v) {
+            return reinterpret_cast<uintptr_t>(v.data) +
+                   static_cast<uintptr_t>(((v.n[0] - 1) * v.s[0] + (v.n[1] - 1) * v.s[1] + v.n[2]) *
+                                          static_cast<int64_t>(elem_bytes(d->dtype)));
+        };
+        const uintptr_t a0 = reinterpret_cast<uintptr_t>(va->data), b0 = reinterpret_cast<uintptr_t>(vb->data);
+        if (a0 < span_end(*vb) && b0 < span_end(*va))
+            return set_error(UHS_EINVAL, "a and b overlap in memory");
+    }
     return check_reach(d, *va);
 }
 
