@@ -208,16 +208,20 @@ int uhs_error_norms_noalloc(const uhs_stencil_desc *desc, const uhs_memref *x, c
 
 /* ---- batches: many programs advanced together -------------------------- */
 /* A batch runs n programs (each its own grids a[i], b[i], descriptor and T)
- * with one persistent kernel launch per timestep: every grid is cut into
- * tiles x z-chunks, and the launch's CTAs walk the combined list, each item
- * swept by its grid's variant (star/box, radius 1-3, rank 2/3, FP64 in float
- * pairs or native, FP32).  uhs_batch_create plans the batch, uploads the
- * per-grid arguments, and captures the whole timestep loop (max T launches;
- * a program stops after its own T) into a CUDA graph; uhs_batch_run replays
- * it on a stream.  Programs the streaming kernels do not cover (generic
- * shapes, UHS_ARITH_EXACT) are rejected with UHS_EUNSUPPORTED.  The grids
- * must stay allocated for the batch's lifetime.  params (may be NULL) applies
- * to every program; only its arith field is used. */
+ * with one persistent kernel launch per timestep.  Every grid is cut into
+ * work items (tile x z-chunk; the z-chunks sized from the batch's total
+ * work so that no item is much longer than a CTA's share), the items are
+ * listed costliest first, and the launch's CTAs take them through an atomic
+ * counter.  Each item is swept by its grid's variant (star/box, radius 1-3,
+ * rank 2/3, FP64 in float pairs or native, FP32; boxes term by term, not as
+ * separable passes).  uhs_batch_create plans the batch, uploads the per-grid
+ * arguments, and captures the whole timestep loop (max T launches; a
+ * program stops after its own T) into a CUDA graph; uhs_batch_run replays
+ * it on any stream and reports through the batch's own status word.
+ * Programs the streaming kernels do not cover (generic shapes,
+ * UHS_ARITH_EXACT) are rejected with UHS_EUNSUPPORTED.  The grids must stay
+ * allocated for the batch's lifetime.  params (may be NULL) applies to every
+ * program; only its arith field is used. */
 typedef struct uhs_batch uhs_batch;
 
 int uhs_batch_create(const uhs_stencil_desc *descs, const uhs_memref *a, const uhs_memref *b, int32_t n,
