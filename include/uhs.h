@@ -177,14 +177,14 @@ int uhs_plan(const uhs_stencil_desc *desc, const uhs_memref *a, const uhs_params
  *   out[2] = out[1] / max |ref|            out[3] = max |ref|
  * x has desc->dtype (F64, F32 or F32X2 pairs); ref is F64 of the same sizes.
  * Returns after the stream drained, with out filled.  Partial sums use
- * scratch memory the library allocates on first use (4 doubles per 64 domain
- * rows, grown as needed, one buffer per device, serialised by a lock). */
+ * scratch memory the library allocates on first use (4 doubles per CTA, at
+ * most 608 CTAs: under 20 KiB, one buffer per device, serialised by a lock).
+ * The sums are FP64; the result does not depend on the device. */
 int uhs_error_norms(const uhs_stencil_desc *desc, const uhs_memref *x, const uhs_memref *ref, double out[4],
                     void *stream);
 
-/* Partial-sum slots of the allocation-free reduction below: it accepts
- * domains of up to UHS_NOALLOC_MAX_PARTIALS * 64 rows (a row is one (z, y)
- * line of the domain; 524288 rows covers a 724^3 interior). */
+/* Partial-sum slots of the allocation-free reduction below.  A reduction
+ * uses at most 608 (one per CTA), so every domain fits. */
 #define UHS_NOALLOC_MAX_PARTIALS 8192
 
 /* No counterpart in the reference.  The same reduction as uhs_error_norms
@@ -196,8 +196,7 @@ int uhs_error_norms(const uhs_stencil_desc *desc, const uhs_memref *x, const uhs
  * synchronisation.  Instead of runtime-owned scratch it uses a fixed array in
  * the library's device memory: 4 * (UHS_NOALLOC_MAX_PARTIALS + 1) doubles,
  * 256 KiB, held on every GPU that loads the library until the process exits.
- * A domain needing more partial slots is rejected with UHS_EUNSUPPORTED.  The
- * call allocates and frees nothing.  Its first call on a device looks up the
+ * The call allocates and frees nothing.  Its first call on a device looks up the
  * array's device address (a one-time set-up), so make that first call before
  * any stream capture.  All calls on a device share the one array; each call
  * rewrites every slot it reads, so nothing carries over between calls, but

@@ -5,21 +5,30 @@
 // of any element type so that FP32 and float-pair results can be scored
 // against an FP64 result without copying either grid back.
 //
-// Two launches: k_err_partial has each CTA reduce ERR_ROWS_PER_BLOCK rows of
-// the domain into one slot of a partials array (sum of squared differences,
-// sum of squared reference values, max |difference|, max |reference|);
-// k_err_final reduces the slots into the result.  The partials array is
-// scratch memory owned by the runtime (grown on demand, one per device).
+// Two launches: k_err_partial has each of at most kErrBlocks CTAs reduce its
+// share of the domain's work units (kErrRowsPerUnit rows, or an x-chunk of
+// them when the rows are few and long) into one slot of a partials array
+// (sum of squared differences, sum of squared reference values,
+// max |difference|, max |reference|); k_err_final reduces the slots into the
+// result.  The partials array is scratch memory owned by the runtime (grown
+// on demand, one per device) or, for the allocation-free entry, a fixed array
+// in the library's device memory.
+//
+// The sums stay in FP64 (3 FP64 operations per point: the difference and two
+// squares), which bounds the kernel by GB300's FP64 pipe rather than HBM;
+// the maxima run on the integer pipes.
 #include <mutex>
 
 #include "uhs_kernels.h"
 
 // Scratch of uhs_error_norms_noalloc: partial sums of up to
-// UHS_NOALLOC_MAX_PARTIALS CTAs plus the 4-double result.  Lives in the
+// UHS_NOALLOC_MAX_PARTIALS CTAs (a reduction uses at most kErrBlocks) plus
+// the 4-double result.  Lives in the
 // library's device memory on every GPU that loads it; host code must not use
 // this name as an address (it is a host-side stand-in): the device address
 // comes from cudaGetSymbolAddress below.
 static __device__ __align__(256) double g_noalloc_scratch[4 * (UHS_NOALLOC_MAX_PARTIALS + 1)];
+static_assert(uhs::kErrBlocks <= UHS_NOALLOC_MAX_PARTIALS, "every reduction fits the allocation-free scratch");
 
 namespace uhs {
 int set_error(int code, const char *fmt, ...);
@@ -30,6 +39,17 @@ namespace {
 
 constexpr int kErrThreads = 256;
 
+// Exact float -> double.  Normal floats and zeros are widened by bit
+// construction on the integer pipes; subnormals, infinities and NaNs (rare)
+// take the conversion instruction.  Same value as static_cast in every case.
+__device__ __forceinline__ double widen(float v) {
+    const unsigned b = __float_as_uint(v), m = b & 0x7fffffffu, s = b & 0x80000000u;
+    if (m - 0x00800000u < 0x7f000000u)
+        return __hiloint2double(static_cast<int>(s | ((m >> 3) + (896u << 20))), static_cast<int>(b << 29));
+    if (m == 0u) return __hiloint2double(static_cast<int>(s), 0);
+    return static_cast<double>(v);
+}
+
 template <class T>
 __device__ __forceinline__ double load_val(const T *p);
 template <>
@@ -38,20 +58,42 @@ __device__ __forceinline__ double load_val<double>(const double *p) {
 }
 template <>
 __device__ __forceinline__ double load_val<float>(const float *p) {
-    return static_cast<double>(*p);
+    return widen(*p);
 }
 template <>
 __device__ __forceinline__ double load_val<float2>(const float2 *p) {
     const float2 v = *p;
-    return static_cast<double>(v.x) + static_cast<double>(v.y);
+    return widen(v.x) + widen(v.y);
 }
+
+// max |v| on the integer pipes.  The bit patterns of non-negative doubles
+// order as their values, so |v| is kept as its (high, low) 32-bit words and
+// compared lexicographically; 64-bit integer compares, and the FP64 min/max,
+// would load the FP64 pipe (a small fraction of the FP32 rate on this part),
+// which then does only the subtraction and the two squares.  A NaN's high
+// word is above kInfHi, or equal to it with a nonzero fraction.
+constexpr unsigned kInfHi = 0x7ff00000u;
+struct AbsMax {
+    unsigned h = 0, l = 0;
+    __device__ __forceinline__ void add(unsigned vh, unsigned vl) {
+        const bool gt = vh > h, eq = vh == h;
+        l = gt ? vl : (eq ? max(l, vl) : l);
+        h = max(h, vh);
+    }
+    __device__ __forceinline__ double value() const {
+        return __hiloint2double(static_cast<int>(h), static_cast<int>(l));
+    }
+};
+__device__ __forceinline__ bool is_nan_words(unsigned h, unsigned l) { return h > kInfHi || (h == kInfHi && l); }
 
 struct ErrArgs {
     const void *x;
     const double *r;
     int64_t xs0, xs1, rs0, rs1;
     int64_t lb0, lb1, lb2, ub0, ub1, ub2;
-    int64_t rows;  // (ub0 - lb0) * (ub1 - lb1)
+    int64_t rows;   // (ub0 - lb0) * (ub1 - lb1)
+    int64_t units;  // row units x xchunks (err_split)
+    int xchunks;
     double *partials;
     double *result;
 };
@@ -86,28 +128,43 @@ __device__ __forceinline__ void block_reduce(double &s2, double &r2, double &md,
     }
 }
 
-// One CTA per ERR_ROWS_PER_BLOCK consecutive (z, y) rows of the domain.
+// Each CTA takes work units blockIdx.x, blockIdx.x + gridDim.x, ...; a unit
+// is kErrRowsPerUnit consecutive (z, y) rows of the domain over one x-chunk.
+// One warp per row at a time, lanes striding along x.  max |x - r| counts a
+// NaN difference as +inf; a NaN reference value does not raise max |r|.
 template <class T>
 __global__ void __launch_bounds__(kErrThreads) k_err_partial(const ErrArgs a) {
     __shared__ double sh[4 * (kErrThreads / 32)];
-    double s2 = 0.0, r2 = 0.0, md = 0.0, mr = 0.0;
+    double s2 = 0.0, r2 = 0.0;
+    AbsMax kd, kr;
     const int64_t ny = a.ub1 - a.lb1;
-    const int64_t row0 = static_cast<int64_t>(blockIdx.x) * kErrRowsPerBlock;
-    const int64_t row1 = min(row0 + kErrRowsPerBlock, a.rows);
+    const int64_t cw = ((a.ub2 - a.lb2 + a.xchunks - 1) / a.xchunks + 31) & ~int64_t(31);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const T *x = static_cast<const T *>(a.x);
-    for (int64_t row = row0; row < row1; ++row) {
-        const int64_t z = a.lb0 + row / ny, y = a.lb1 + row % ny;
-        const T *xr = x + z * a.xs0 + y * a.xs1;
-        const double *rr = a.r + z * a.rs0 + y * a.rs1;
-        for (int64_t i = a.lb2 + threadIdx.x; i < a.ub2; i += kErrThreads) {
-            const double rv = rr[i];
-            const double d = load_val<T>(xr + i) - rv;
-            s2 = fma(d, d, s2);
-            r2 = fma(rv, rv, r2);
-            md = fmax(md, d != d ? __longlong_as_double(0x7ff0000000000000ll) : fabs(d));
-            mr = fmax(mr, fabs(rv));
+    for (int64_t u = blockIdx.x; u < a.units; u += gridDim.x) {
+        const int64_t row0 = (u / a.xchunks) * kErrRowsPerUnit, row1 = min(row0 + kErrRowsPerUnit, a.rows);
+        const int64_t x0 = a.lb2 + (u % a.xchunks) * cw, x1 = min(x0 + cw, a.ub2);
+        for (int64_t row = row0 + warp; row < row1; row += kErrThreads / 32) {
+            const int64_t z = a.lb0 + row / ny, y = a.lb1 + row % ny;
+            const T *xr = x + z * a.xs0 + y * a.xs1;
+            const double *rr = a.r + z * a.rs0 + y * a.rs1;
+#pragma unroll 4
+            for (int64_t i = x0 + lane; i < x1; i += 32) {
+                const double rv = rr[i];
+                const double d = load_val<T>(xr + i) - rv;
+                s2 = fma(d, d, s2);
+                r2 = fma(rv, rv, r2);
+                const unsigned dh = static_cast<unsigned>(__double2hiint(d)) & 0x7fffffffu;
+                const unsigned dl = static_cast<unsigned>(__double2loint(d));
+                const unsigned rh = static_cast<unsigned>(__double2hiint(rv)) & 0x7fffffffu;
+                const unsigned rl = static_cast<unsigned>(__double2loint(rv));
+                if (is_nan_words(dh, dl)) kd.add(kInfHi, 0u);
+                else kd.add(dh, dl);
+                if (!is_nan_words(rh, rl)) kr.add(rh, rl);
+            }
         }
     }
+    double md = kd.value(), mr = kr.value();
     block_reduce(s2, r2, md, mr, sh);
     if (threadIdx.x == 0) {
         double *p = a.partials + 4 * static_cast<int64_t>(blockIdx.x);
@@ -153,6 +210,8 @@ cudaError_t launch_error_norms(const ErrNormsCall &c) {
     a.ub1 = c.ub[1];
     a.ub2 = c.ub[2];
     a.rows = (c.ub[0] - c.lb[0]) * (c.ub[1] - c.lb[1]);
+    a.units = c.units;
+    a.xchunks = c.xchunks > 0 ? c.xchunks : 1;
     a.partials = c.scratch;
     a.result = c.scratch + 4 * static_cast<int64_t>(c.nblocks);
     if (c.dtype == UHS_F64) k_err_partial<double><<<c.nblocks, kErrThreads, 0, c.stream>>>(a);
@@ -198,12 +257,9 @@ extern "C" int uhs_error_norms_noalloc(const uhs_stencil_desc *d, const uhs_memr
         out[0] = out[1] = out[2] = out[3] = 0.0;
         return UHS_OK;
     }
-    if (c.nblocks > UHS_NOALLOC_MAX_PARTIALS)
-        return uhs::set_error(UHS_EUNSUPPORTED,
-                              "the domain has %lld rows and needs %d partial slots; the allocation-free reduction "
-                              "holds %d (domains of up to %d rows): use uhs_error_norms",
-                              (long long)((d->ub[0] - d->lb[0]) * (d->ub[1] - d->lb[1])), c.nblocks,
-                              UHS_NOALLOC_MAX_PARTIALS, UHS_NOALLOC_MAX_PARTIALS * uhs::kErrRowsPerBlock);
+    if (c.nblocks > UHS_NOALLOC_MAX_PARTIALS)  // cannot happen: err_split caps CTAs at kErrBlocks
+        return uhs::set_error(UHS_EUNSUPPORTED, "the reduction needs %d partial slots; the allocation-free "
+                              "scratch holds %d", c.nblocks, UHS_NOALLOC_MAX_PARTIALS);
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return uhs::set_error(UHS_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(e));

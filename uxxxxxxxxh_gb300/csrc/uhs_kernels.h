@@ -47,16 +47,35 @@ unsigned *stream_error_word(int device, cudaStream_t stream);
 cudaError_t launch_generic(const SweepSpec &sp, const LaunchCfg &cfg, const GridView &in,
                            const GridView &out, cudaStream_t st);
 
-// FP64 error reduction (error_norms.cu): one CTA per kErrRowsPerBlock rows
-// of the domain writes 4 doubles of partials into scratch; the result (4
-// doubles) follows the partials.  Scratch holds 4 * (nblocks + 1) doubles.
-constexpr int kErrRowsPerBlock = 64;
+// FP64 error reduction (error_norms.cu).  The domain is cut into work units
+// of kErrRowsPerUnit rows (and, when that gives too few units to balance the
+// GPU -- few long rows, as in 2D grids -- into x-chunks of at least 256
+// elements); at most kErrBlocks CTAs take the units round-robin, each writing
+// 4 doubles of partials into scratch; the result (4 doubles) follows the
+// partials.  Scratch holds 4 * (nblocks + 1) doubles.  The split depends only
+// on the domain's shape, so results are the same on every device.
+constexpr int kErrRowsPerUnit = 16;
+constexpr int64_t kErrBlocks = 4 * 152;  // 4 resident 256-thread CTAs per SM
+inline void err_split(int64_t rows, int64_t width, int64_t *units, int *xchunks, int *nblocks) {
+    const int64_t ru = (rows + kErrRowsPerUnit - 1) / kErrRowsPerUnit, want = 8 * kErrBlocks;
+    int64_t xc = 1;
+    if (ru > 0 && ru < want) {
+        const int64_t a = (want + ru - 1) / ru, b = (width + 255) / 256;
+        xc = a < b ? a : b;
+        if (xc < 1) xc = 1;
+    }
+    *units = ru * xc;
+    *xchunks = static_cast<int>(xc);
+    *nblocks = static_cast<int>(*units < kErrBlocks ? *units : kErrBlocks);
+}
 struct ErrNormsCall {
     int dtype;   // element type of x
     GridView x;  // grid under test
     GridView r;  // FP64 reference grid
     int64_t lb[3], ub[3];
-    int nblocks;
+    int nblocks;    // CTAs = partial slots (err_split)
+    int xchunks;    // x-chunks per row unit
+    int64_t units;  // row units x xchunks
     double *scratch;
     cudaStream_t stream;
 };

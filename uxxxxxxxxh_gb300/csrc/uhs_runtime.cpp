@@ -825,8 +825,7 @@ int prepare_error_norms(const uhs_stencil_desc *d, const uhs_memref *x, const uh
         c->lb[i] = d->lb[i];
         c->ub[i] = d->ub[i];
     }
-    const int64_t nblocks = *empty ? 0 : (rows + kErrRowsPerBlock - 1) / kErrRowsPerBlock;
-    c->nblocks = static_cast<int>(std::min<int64_t>(nblocks, int64_t(1) << 30));
+    if (!*empty) err_split(rows, d->ub[2] - d->lb[2], &c->units, &c->xchunks, &c->nblocks);
     return UHS_OK;
 }
 
@@ -1207,8 +1206,9 @@ int uhs_error_norms(const uhs_stencil_desc *d, const uhs_memref *x, const uhs_me
         out[0] = out[1] = out[2] = out[3] = 0.0;
         return UHS_OK;
     }
-    const int64_t nblocks = (rows + kErrRowsPerBlock - 1) / kErrRowsPerBlock;
-    if (nblocks > (int64_t(1) << 30)) return set_error(UHS_EUNSUPPORTED, "domain too large for the reduction");
+    int64_t units = 0;
+    int xchunks = 1, nblocks = 0;
+    err_split(rows, d->ub[2] - d->lb[2], &units, &xchunks, &nblocks);
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64) return set_error(UHS_EUNSUPPORTED, "device ordinal %d", dev);
@@ -1237,7 +1237,9 @@ int uhs_error_norms(const uhs_stencil_desc *d, const uhs_memref *x, const uhs_me
         c.lb[i] = d->lb[i];
         c.ub[i] = d->ub[i];
     }
-    c.nblocks = static_cast<int>(nblocks);
+    c.nblocks = nblocks;
+    c.xchunks = xchunks;
+    c.units = units;
     c.scratch = buf[dev];
     c.stream = static_cast<cudaStream_t>(stream);
     cudaError_t e = launch_error_norms(c);
