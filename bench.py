@@ -53,6 +53,7 @@ def parse_args():
     p.add_argument("--dtype", choices=["f64", "f32"], default="f64", help="grid element type of the main run")
     p.add_argument("--arith", type=int, default=0)
     p.add_argument("--kernel", type=int, default=0)
+    p.add_argument("--ktemporal", type=int, default=0, help="temporal fusion depth of the main run (1, 2, 4)")
     p.add_argument("--no-cpu", action="store_true", help="skip the oracle (profiling runs)")
     p.add_argument("--no-fp32", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -438,7 +439,8 @@ def main():
         dist = dist_mod
 
     st, a0 = make_workload(args)
-    params = uhs.RunParams(kernel=args.kernel, arith=args.arith, flags=uhs._lib.UHS_FLAG_NO_SYNC)
+    params = uhs.RunParams(kernel=args.kernel, arith=args.arith, k_temporal=args.ktemporal,
+                           flags=uhs._lib.UHS_FLAG_NO_SYNC)
     stream = torch.cuda.Stream()
     tdt = torch.float32 if st.dtype == uhs.UHS_F32 else torch.float64
     dev_a = torch.from_numpy(a0.reshape(st.sizes)).to(tdt).cuda()
@@ -483,7 +485,7 @@ def main():
         oracle.iterate_f64(st, ra, rb)
         dev_a.copy_(torch.from_numpy(a0.reshape(st.sizes)))
         dev_b.copy_(dev_a)
-        uhs.run(st, dev_a, dev_b, uhs.RunParams(kernel=args.kernel, arith=args.arith))
+        uhs.run(st, dev_a, dev_b, uhs.RunParams(kernel=args.kernel, arith=args.arith, k_temporal=args.ktemporal))
         got = dev_a.double().cpu().numpy().reshape(-1)
         errs = oracle.error(st, ra, got)
         errs["halo_bit_exact"] = oracle.halo_diff(st, ra, got) == 0
@@ -506,6 +508,19 @@ def main():
             e = oracle.error(st, ra, a32.cpu().numpy().reshape(-1))
             fp32["l2_rel_vs_f64_oracle"] = e["l2_rel"]
             fp32["max_rel_vs_f64_oracle"] = e["max_rel"]
+        # The same comparison at full size on the GPU (uhs.error_norms): the
+        # FP32 result against this library's FP64 sweep of the same rounded
+        # input, which itself is within 1e-12 of the oracle.
+        rounded = torch.from_numpy(a0.astype(np.float32).reshape(st.sizes))
+        dev_a.copy_(rounded)
+        dev_b.copy_(dev_a)
+        uhs.run(st, dev_a, dev_b, uhs.RunParams(kernel=args.kernel, arith=args.arith, k_temporal=args.ktemporal))
+        a32.copy_(rounded)
+        b32.copy_(a32)
+        uhs.run(st32, a32, b32)
+        e = uhs.error_norms(st32, a32, dev_a)
+        fp32["l2_rel_vs_f64_gpu"] = e["l2_rel"]
+        fp32["max_rel_vs_f64_gpu"] = e["max_rel"]
         del a32, b32
 
     # End to end through the C ABI with host buffers.
