@@ -201,6 +201,7 @@ struct Plan {
     LaunchCfg cfg;
     // streaming kernel
     int shape = -1, R = 0, st = 0, ar = 0, ld = kLdCpAsync, tile = 0, zchunk = 0;
+    int zcap = 0;              // default launches: upper bound on the automatic z-chunk (0: none)
     std::vector<double> coef;  // coef_slot order
     bool auto_df32 = false;    // df32 chosen by UHS_ARITH_AUTO, subject to range_ok()
     bool factored = false;     // separable box run as 1D passes
@@ -408,23 +409,35 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
     pl->st = sp.dtype == UHS_F64 ? kStF64 : sp.dtype == UHS_F32 ? kStF32 : kStF32x2;
     pl->ar = arith == UHS_ARITH_DF32 ? kArDf32 : kArNative;
     const bool is2d = sp.rank == 2;
+    // separable boxes run as 1D passes unless the caller opts out
+    std::vector<double> fac;
+    const bool sep = (shape == kBox3 || shape == kBox2) && !(p->flags & UHS_FLAG_NO_FACTOR) && factor_box(sp, R, &fac);
     // tile variant from (tile_x, tile_y, vy)
     int tile = 0;
+    pl->zcap = 0;
     if (is2d) {
         if (cfg.tile_x == 64) tile = 1;
         else if (cfg.tile_x == 256) tile = 2;
         else if (cfg.tile_x != 0 && cfg.tile_x != 128)
             return set_error(UHS_EINVAL, "rank-2 streaming tiles are 64, 128 or 256 wide (got %d)", cfg.tile_x);
+        // FP32 rows: 256-wide strips (cp.async), 2-30 % over 128 on the
+        // twelve reference shapes at 8192^2; float pairs keep 128
+        if (cfg.tile_x == 0 && sp.dtype == UHS_F32 && arith != UHS_ARITH_DF32) tile = 2;
     } else if (cfg.tile_x == 0 && cfg.tile_y == 0 && p->vy == 0) {
-        // measured on GB300 (512^3): df32 fastest at 64 x 8; native FP32 at
-        // 32 x 32, with 8 points per thread for stars of radius 2-3 on grids
-        // of 256 rows or more (3d3r: 408 vs 340 GStencil/s at 4 points;
-        // fewer rows leave too few 32-row tiles)
-        // Float-pair stars of radius 2-3 prefer 32 x 16 with 4 points per
-        // thread (3d3r: 88.5 vs 82.7 GStencil/s at 64 x 8).
-        const bool vy8 = sp.dtype == UHS_F32 && shape == kStar3 && R >= 2 && sp.ub[1] - sp.lb[1] >= 256;
-        if (arith == UHS_ARITH_DF32) tile = (shape == kStar3 && R >= 2) ? 1 : 2;
-        else tile = vy8 ? 4 : 0;
+        // Defaults from planner-against-exhaustive-tuning runs on GB300 at
+        // 512^3 (studies.py shapes, reference and random coefficients).
+        // Tiles: 0 = 32 x 32 points, 4 per thread along y; 1 = 32 x 16, 4 per
+        // thread; 2 = 64 x 8, 2 per thread (big boxes, r2-3 term by term,
+        // have one fixed tile).  GStencil/s new vs old default, z-chunk caps
+        // (below) included.
+        if (arith == UHS_ARITH_DF32) {
+            if (shape == kStar3) tile = R >= 2 ? 1 : 2;  // 3d2r 118.4 vs 114.7
+            else if (sep) tile = R == 2 ? 1 : 0;         // 3d1r/2r/3r 147/97/64 vs 137/77/52 at 64 x 8
+            else tile = 1;                               // 3d1r box 81.6 vs 75.9
+        } else if (sp.dtype == UHS_F32) {
+            if (shape == kStar3) tile = R == 2 ? 0 : 1;  // 3d1r/2r/3r 632/659/438 vs 596/625/410
+            else if (sep) tile = 1;                      // 3d1r/2r/3r 626/563/297 vs 588/548/270 at 32 x 32
+        }  // non-separable FP32 boxes and native FP64 keep tile 0
     } else {
         if (cfg.tile_x == 64) tile = 2;
         else if (cfg.tile_x != 0 && cfg.tile_x != 32)
@@ -438,6 +451,17 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
         }
     }
     pl->tile = tile;
+    // Upper bound on the automatic z-chunk (about four waves of CTAs) for 3D
+    // sweeps: shorter chunks measured faster in these classes (FP32 3d1r
+    // star 632 vs 596 GStencil/s at 16 planes; float-pair 3d3r box 6.8 vs
+    // 6.3 at 16; float-pair 3d2r star 118.4 vs 114.7 at 64).  A caller's
+    // tile_z overrides it.
+    if (!is2d) {
+        const bool df = arith == UHS_ARITH_DF32, f32 = sp.dtype == UHS_F32 && !df;
+        if (shape == kStar3) pl->zcap = df ? (R >= 2 ? 64 : 0) : f32 ? (R == 3 ? 64 : 16) : 0;
+        else if (sep) pl->zcap = (df || f32) ? (R >= 2 ? 64 : f32 ? 16 : 0) : 0;
+        else pl->zcap = df ? (R >= 2 ? 16 : 64) : f32 ? (R >= 2 ? 64 : 0) : 0;
+    }
     // the kernel keeps in-plane offsets in 32 bits
     const int64_t plane_elems = is2d ? view.s[1] : view.s[0];
     if (plane_elems >= (int64_t(1) << 31) || view.n[2] >= (int64_t(1) << 31)) {
@@ -451,14 +475,15 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
     // loader
     const int eb = sp.dtype == UHS_F32 ? 4 : 8;
     bool tma_ok = cfg.use_tma >= 0 && !(is2d && tile == 2);
+    // float-pair 2D boxes term by term load faster by cp.async (2d2r box at
+    // 8192^2: 71.8 vs 65.6 GStencil/s with TMA)
+    if (cfg.use_tma == 0 && is2d && shape == kBox2 && !sep && arith == UHS_ARITH_DF32) tma_ok = false;
     const int64_t row_b = (is2d ? view.s[1] : view.s[1]) * eb, plane_b = (is2d ? view.s[1] : view.s[0]) * eb;
     if (reinterpret_cast<uintptr_t>(view.data) % 16 || row_b % 16 || plane_b % 16) tma_ok = false;
     if (cfg.use_tma > 0 && !tma_ok)
         return set_error(UHS_EUNSUPPORTED, "TMA needs 16-byte aligned grids and row/plane strides");
     pl->ld = tma_ok ? kLdTma : kLdCpAsync;
-    // separable boxes run as 1D passes unless the caller opts out
-    std::vector<double> fac;
-    if ((shape == kBox3 || shape == kBox2) && !(p->flags & UHS_FLAG_NO_FACTOR) && factor_box(sp, R, &fac)) {
+    if (sep) {
         pl->shape = shape = (shape == kBox3) ? kSep3 : kSep2;
         pl->coef = fac;
         pl->factored = true;
@@ -628,7 +653,10 @@ static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in,
             c.ld = kLdCpAsync;
         }
     }
-    // z-chunk: enough CTAs for about four waves over the SMs
+    // z-chunk: enough CTAs for about four waves over the SMs, at most the
+    // planner's cap; at least 32 rows for rank-2 strips (2048^2 to 4096^2
+    // FP32 5-point: 340 / 507 GStencil/s at 32 rows against 291 / 454 at the
+    // 8 rows four waves would give)
     int bx, by;
     stream_tile_xy(c, &bx, &by);
     const int64_t nz = c.ub[0] - c.lb[0];
@@ -641,7 +669,9 @@ static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in,
         if (stream_dispatch(q) != cudaSuccess || occ <= 0) occ = 1;
         const int64_t want = static_cast<int64_t>(device_sms()) * occ * 4;
         const int64_t chunks = std::max<int64_t>(1, (want + tiles - 1) / tiles);
-        zchunk = static_cast<int>(std::max<int64_t>(std::max(8, 4 * c.R), (nz + chunks - 1) / chunks));
+        const int floor_z = std::max(sp.rank == 2 ? 32 : 8, 4 * c.R);
+        zchunk = static_cast<int>(std::max<int64_t>(floor_z, (nz + chunks - 1) / chunks));
+        if (pl.zcap > 0) zchunk = std::min(zchunk, std::max(pl.zcap, floor_z));
     }
     c.zchunk = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(zchunk > 0 ? zchunk : 1, std::max<int64_t>(nz, 1))));
     // 4-byte grids: copy in 8-byte pairs when every row start of the tile is 8-byte aligned

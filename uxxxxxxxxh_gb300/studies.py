@@ -7,7 +7,8 @@ shapes: the 12 reference cases at the reference GPU harness's own sizes
 1-3 cell halos), each in FP64 float pairs, native FP64 and FP32, launched with
 the exhaustive tuner's best configuration for that exact program; reported as
 GStencil/s beside the reference's published A100 figure for the same case
-(scripts/figure_scripts/data.xlsx, sheet GPU, as ns per sweep).
+(scripts/figure_scripts/data.xlsx, sheet GPU, as ns per sweep).  Each row also
+times the planner's own choice (no tuner database) against that best.
 
 Coefficients: by default seeded random ones (no two alike, so no box
 factors into 1D passes -- the general case); with --programs, the programs
@@ -20,6 +21,7 @@ therefore lives with the tests (tests/test_precision_gpu.py).
 from __future__ import annotations
 
 import argparse
+from dataclasses import asdict
 import json
 import os
 import sys
@@ -27,7 +29,7 @@ import sys
 from . import _lib
 from .runtime import RunParams, memref_raw, plan
 from .stencil import Stencil, box_offsets, make_stencil, star_offsets
-from .tuner import Tuner, device_grids
+from .tuner import Tuner, device_grids, measure
 from .workloads import normalised, splitmix_uniform
 
 # Reference A100 ns per sweep (UHStencil, FP64, 8192^2 / 512^3), data.xlsx sheet GPU.
@@ -68,7 +70,13 @@ def shapes_study(out: str | None = None, reps: int = 3, programs_path: str | Non
                                             params=RunParams(flags=_lib.UHS_FLAG_NO_TUNE_DB)).factored
             a, b = device_grids(st)
             t = Tuner()
-            _, results = t.tune(st, a, b, reps=reps, push=False)
+            best, results = t.tune(st, a, b, reps=reps, push=False)
+            row[f"{label}_best"] = {k: v for k, v in asdict(best).items() if v and k != "flags"}
+            # the planner's own choice (no tuner database), timed the same way
+            dflt = plan(st, memref_raw(1 << 20, st.sizes), params=RunParams(flags=_lib.UHS_FLAG_NO_TUNE_DB))
+            dflt.flags = _lib.UHS_FLAG_NO_TUNE_DB
+            row[f"{label}_default_gst"] = 1.0 / min(measure(st, a, b, dflt, reps=reps) for _ in range(2))
+            row[f"{label}_default"] = {k: v for k, v in asdict(dflt).items() if v and k != "flags"}
             if dtype == _lib.UHS_F64:
                 df = [1.0 / ns_ for ns_, p in results if p.arith == _lib.UHS_ARITH_DF32]
                 nat = [1.0 / ns_ for ns_, p in results if p.arith != _lib.UHS_ARITH_DF32]
@@ -79,6 +87,8 @@ def shapes_study(out: str | None = None, reps: int = 3, programs_path: str | Non
             del a, b
         row["f64_best_vs_a100"] = max(row["f64_df32_gst"] or 0, row["f64_native_gst"] or 0) / row["a100_gst"]
         row["f32_vs_f64"] = row["f32_gst"] / max(row["f64_df32_gst"] or 0, row["f64_native_gst"] or 0)
+        row["f64_default_vs_best"] = row["f64_default_gst"] / max(row["f64_df32_gst"] or 0, row["f64_native_gst"] or 0)
+        row["f32_default_vs_best"] = row["f32_default_gst"] / row["f32_gst"]
         rows.append(row)
         print(json.dumps(row), flush=True)
     res = {"study": "shapes", "coefficients": "reference" if programs is not None else "random", "rows": rows}

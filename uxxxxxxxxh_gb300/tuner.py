@@ -14,8 +14,8 @@ record for the learned cost model (costmodel.py).
 Candidates (rank 3): tile {32x32 VY4, 32x16 VY4, 64x8 VY2, 32x16 VY2, and for
 FP32 stars 32x32 VY8} x
 loader {TMA, cp.async} x z-chunk {auto, 16, 64} x arithmetic (FP64:
-{float pairs, native}); rank 2: rows {64, 128, 256} x loader x z-chunk
-{auto, 128, 512} x arithmetic; plus the generic kernel, and on request
+{float pairs, native}); rank 2: rows {64, 128, 256} x loader x row chunk
+{auto, 64, 128} x arithmetic; plus the generic kernel, and on request
 (include_mma) for FP32 3D boxes of radius 2 and 3 the tensor-core kernel (16
 or 32 columns).  Candidates that plan to the same launch are timed once.
 """
@@ -94,7 +94,7 @@ def candidates(st: Stencil, include_mma: bool = False) -> list:
         ([_lib.UHS_ARITH_DF32] if st.dtype == _lib.UHS_F32X2 else [_lib.UHS_ARITH_FMA])
     tiles = [dict(tile_x=t[0], tile_y=t[1], vy=t[2]) for t in TILES3] if st.rank == 3 else \
         [dict(tile_x=t) for t in TILES2]
-    zs = [0, 16, 64] if st.rank == 3 else [0, 128, 512]
+    zs = [0, 16, 64] if st.rank == 3 else [0, 64, 128]
     raw = [RunParams(kernel=STREAM, arith=ar, use_tma=tma, tile_z=tz, flags=_lib.UHS_FLAG_NO_TUNE_DB, **t)
            for ar in ariths for t in tiles for tma in (1, -1) for tz in zs]
     if st.dtype != _lib.UHS_F32X2:
