@@ -17,7 +17,8 @@ Reported (one JSON line, rank 0):
   cpu_baseline  the oracle's restatement of the reference's serial loops on
              this host's cores, on a bounded sample of the same workload
   fp32       the same workload on FP32 grids, with its L2 error against the
-             FP64 oracle (the FP32-vs-FP64 comparison)
+             FP64 oracle and, at full size on the GPU, against this library's
+             FP64 sweep of the same rounded input (uhs.error_norms)
 Inputs (1.09 GB per grid) are larger than the 129 MB L2, so no flush is
 needed between timed iterations.
 
@@ -76,6 +77,14 @@ def load_peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def load_bf16_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return float(json.load(f)["bf16_tflops"])
+    return 1900.0
 
 
 def make_workload(args):
@@ -254,8 +263,20 @@ def box_paths(uhs, args, stream):
         b.copy_(a)
         uhs.run(s, a, b, p)
         e = oracle.error(st, ra, a.double().cpu().numpy().reshape(-1))
-        out[name] = {"gstencil_s": st.interior_points * st.iterations * max(1, args.steps) / (ms * 1e-3) / 1e9,
-                     "l2_rel": e["l2_rel"], "max_rel": e["max_rel"], "kernel": uhs.plan(s, a, p).kernel}
+        q = uhs.plan(s, a, p)
+        gst = st.interior_points * st.iterations * max(1, args.steps) / (ms * 1e-3) / 1e9
+        out[name] = {"gstencil_s": gst, "l2_rel": e["l2_rel"], "max_rel": e["max_rel"], "kernel": q.kernel}
+        if q.kernel == F.UHS_KERNEL_MMA:
+            # Tensor-core rate: each output column takes K = tile_x + 8 window
+            # columns per (dz, dy) row shift and three split-tf32 MMAs (hi.hi,
+            # lo.hi, hi.lo); useful work is 2P flops per point.  Dense tf32
+            # runs at half the bf16 rate, so the peak is half the measured bf16.
+            d = 2 * max(st.radius) + 1
+            issued = gst * 2 * (q.tile_x + 8) * d * d * 3 / 1e3
+            peak = load_bf16_peak() / 2
+            out[name]["tensor"] = {"useful_tflops": gst * 2 * len(st.terms) / 1e3, "issued_tflops": issued,
+                                   "tf32_peak_tflops": peak, "frac": issued / peak,
+                                   "peak_source": "half the measured bf16 dense rate (MEASURED_PEAKS.json)"}
         del a, b
     return out
 
