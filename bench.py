@@ -10,7 +10,9 @@ Reported (one JSON line, rank 0):
   value      GStencil/s = interior points * T / time, grids resident in HBM
   e2e        the same metric through the C ABI with host buffers: pinned host
              -> device copy of the input grid, the run, device -> host copy of
-             the result, all inside the timed region
+             the result, all inside the timed region, with two runs in flight
+             on two streams (one run's copies overlap the other's sweeps);
+             e2e_serial is the same with one run at a time
   roofline   the sweep kernel's algorithmic bytes (16 B per point-update for
              FP64: one read and one write) per launch over its average launch
              time, against the measured HBM copy bandwidth
@@ -544,12 +546,22 @@ def main():
         fp32["max_rel_vs_f64_gpu"] = e["max_rel"]
         del a32, b32
 
-    # End to end through the C ABI with host buffers.
-    e2e = None
+    # End to end through the C ABI with host buffers: each step copies its
+    # input grid from pinned host memory, runs the program (uhs_run) and reads
+    # the result back.  Measured twice: with one run at a time on one stream,
+    # and with two runs in flight on two streams (each its own device grids
+    # and host result buffer), so that one run's copies overlap the other's
+    # sweeps -- how a service streaming independent grids would drive it.
+    e2e = e2e_serial = None
     if not args.no_e2e:
         host_in = torch.from_numpy(a0.reshape(st.sizes)).to(tdt).pin_memory()
-        host_out = torch.empty_like(host_in).pin_memory()
-        with torch.cuda.stream(stream):
+        nbytes = host_in.numel() * host_in.element_size()
+
+        def e2e_run(nstreams: int) -> float:
+            streams = [stream] + [torch.cuda.Stream() for _ in range(nstreams - 1)]
+            grids = [(dev_a, dev_b)] + [(torch.empty_like(dev_a), torch.empty_like(dev_a))
+                                        for _ in range(nstreams - 1)]
+            outs = [torch.empty_like(host_in).pin_memory() for _ in range(nstreams)]
             for it in range(args.warmup + args.steps):
                 if it == args.warmup:
                     torch.cuda.synchronize()
@@ -557,17 +569,33 @@ def main():
                         dist.barrier()
                     f0 = torch.cuda.Event(enable_timing=True)
                     f1 = torch.cuda.Event(enable_timing=True)
-                    f0.record(stream)
-                dev_a.copy_(host_in, non_blocking=True)
-                dev_b.copy_(dev_a, non_blocking=True)
-                uhs.run(st, dev_a, dev_b, params, stream=stream)
-                host_out.copy_(dev_a, non_blocking=True)
-            f1.record(stream)
+                    f0.record(streams[0])
+                    for s in streams[1:]:
+                        s.wait_event(f0)
+                k = it % nstreams
+                s, (ga, gb) = streams[k], grids[k]
+                with torch.cuda.stream(s):
+                    ga.copy_(host_in, non_blocking=True)
+                    gb.copy_(ga, non_blocking=True)
+                    uhs.run(st, ga, gb, params, stream=s)
+                    outs[k].copy_(ga, non_blocking=True)
+            for s in streams[1:]:
+                ev = torch.cuda.Event()
+                ev.record(s)
+                streams[0].wait_event(ev)
+            f1.record(streams[0])
             torch.cuda.synchronize()
-        ems = reduce_max_ms(f0.elapsed_time(f1), dist, "cuda")
-        nbytes = host_in.numel() * host_in.element_size()
-        e2e = {"value": aggregate_gst(pts, args.steps, ems, world), "unit": "GStencil/s",
-               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": ems / args.steps}
+            return reduce_max_ms(f0.elapsed_time(f1), dist, "cuda")
+
+        for label, nstreams in (("serial", 1), ("overlapped", 2)):
+            ems = e2e_run(nstreams)
+            rec = {"value": aggregate_gst(pts, args.steps, ems, world), "unit": "GStencil/s",
+                   "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": ems / args.steps,
+                   "runs_in_flight": nstreams}
+            if label == "serial":
+                e2e_serial = rec
+            else:
+                e2e = rec
 
     if rank != 0:
         return
@@ -600,6 +628,7 @@ def main():
         "sweep_launches": sweeps,
         "clocks": clk,
         "e2e": e2e,
+        "e2e_serial": e2e_serial,
         "cpu_baseline": cpu,
         "error_vs_oracle": errs,
         "fp32": fp32,
