@@ -1,0 +1,81 @@
+"""The planner's default launches (no parameters, no tuner database), planned
+on the host: the per-class tiles chosen from timing the defaults against
+exhaustive tuning on GB300, and that a caller's tile overrides them.  The
+z-chunk caps act at launch time; `tile_z` stays 0 (automatic) in the plan."""
+import pytest
+
+from uxxxxxxxxh_gb300 import _lib
+from uxxxxxxxxh_gb300.runtime import RunParams, memref_raw, plan
+from uxxxxxxxxh_gb300.stencil import box_offsets, make_stencil
+from uxxxxxxxxh_gb300.workloads import cfg3, random_case
+
+F = _lib
+NO_DB = RunParams(flags=F.UHS_FLAG_NO_TUNE_DB)
+
+
+def planned(st):
+    p = plan(st, memref_raw(1 << 20, st.sizes), params=NO_DB)
+    return p.tile_x, p.tile_y, p.vy
+
+
+def separable_box(r, dtype):
+    """A rank-1 box (the planner sweeps it as 1D passes)."""
+    w = [1.0 + abs(d) for d in range(-r, r + 1)]
+    offs = box_offsets(3, r)
+    coefs = [w[dz + r] * w[dy + r] * w[dx + r] / sum(w) ** 3 for dz, dy, dx in offs]
+    return make_stencil(f"sep{r}", 3, (96, 96, 96), r, offs, coefs, dtype=dtype)
+
+
+@pytest.mark.parametrize("r,want", [(1, (64, 8, 2)), (2, (32, 16, 4)), (3, (32, 16, 4))])
+def test_float_pair_stars(r, want):
+    st, _ = random_case(3, r, "star", (64, 64, 64), 2, 1)
+    assert planned(st) == want
+
+
+@pytest.mark.parametrize("r,want", [(1, (32, 32, 4)), (2, (32, 16, 4)), (3, (32, 32, 4))])
+def test_float_pair_separable_boxes(r, want):
+    st = separable_box(r, F.UHS_F64)
+    assert plan(st, memref_raw(1 << 20, st.sizes), params=NO_DB).factored == 1
+    assert planned(st) == want
+
+
+def test_float_pair_term_by_term_boxes():
+    st, _ = random_case(3, 1, "box", (64, 64, 64), 2, 2)
+    assert planned(st) == (32, 16, 4)
+    st, _ = random_case(3, 3, "box", (64, 64, 64), 2, 3)
+    assert planned(st) == (32, 16, 2)  # radius 2-3 boxes have one tile
+
+
+@pytest.mark.parametrize("r,rows,want", [(1, 512, (32, 16, 4)), (2, 512, (32, 32, 4)), (2, 294, (32, 16, 4)),
+                                         (3, 512, (32, 16, 4))])
+def test_fp32_stars(r, rows, want):
+    """Radius 2 takes 32-row tiles only when they leave at most 2 % of the
+    rows idle (294 rows: 10 tiles of 32 would cover 320)."""
+    st, _ = random_case(3, r, "star", (64, rows, 96), 2, 4, dtype=F.UHS_F32)
+    assert planned(st) == want
+
+
+def test_fp32_separable_box_and_2d_strips():
+    st, _ = cfg3(n=64)
+    st = st.with_(dtype=F.UHS_F32)
+    assert planned(st) == (32, 16, 4)
+    for r, kind in ((1, "star"), (3, "box")):
+        st, _ = random_case(2, r, kind, (300, 700), 2, 5, dtype=F.UHS_F32)
+        assert planned(st)[0] == 256
+        st64 = st.with_(dtype=F.UHS_F64)
+        assert planned(st64)[0] == 128
+
+
+def test_float_pair_2d_term_by_term_boxes_load_by_cp_async():
+    st, _ = random_case(2, 2, "box", (300, 700), 2, 6)
+    p = plan(st, memref_raw(1 << 20, st.sizes), params=NO_DB)
+    assert p.use_tma == -1
+    star, _ = random_case(2, 2, "star", (300, 700), 2, 6)
+    assert plan(star, memref_raw(1 << 20, star.sizes), params=NO_DB).use_tma == 1
+
+
+def test_caller_tiles_override_the_defaults():
+    st, _ = random_case(3, 1, "star", (64, 64, 64), 2, 7)
+    p = plan(st, memref_raw(1 << 20, st.sizes),
+             params=RunParams(tile_x=32, tile_y=32, vy=4, tile_z=24, flags=F.UHS_FLAG_NO_TUNE_DB))
+    assert (p.tile_x, p.tile_y, p.vy, p.tile_z) == (32, 32, 4, 24)
