@@ -395,7 +395,12 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
     unsigned phase = 0;  // mbarrier phase of plane j's slot
     int s_iss = PD % NSTG;
     int s_cmp = 0;  // compute-ring slot of plane j
-#pragma unroll 1
+    // Radius-1 stars: three copies of the plane step, the length of the
+    // z-queue, so its shifts become register renaming (GB300: 3d7pt float
+    // pairs 175.4 -> 179.8 GStencil/s, 2d5pt 176.4 -> 182.3, FP32 490 -> 511
+    // in 2D).  Longer queues gain nothing and raise register use.
+    constexpr int UNROLL_Q = (STAR && R == 1) ? 3 : 1;
+#pragma unroll UNROLL_Q
     for (int j = 0; j < nq; ++j) {
         bool ok = true;
         if constexpr (C::LD == kLdCpAsync) {
