@@ -344,6 +344,7 @@ def bench_batch(args, rank: int, world: int, local: int):
         batch.run(stream, sync=False)
     e1.record(stream)
     torch.cuda.synchronize()
+    launches = uhs.launch_count() - n0
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
     pts = sum(st.interior_points * st.iterations for st, _ in specs)
@@ -363,7 +364,7 @@ def bench_batch(args, rank: int, world: int, local: int):
                        "work_items_per_timestep": st_["items"], "l2": f"{sum(2 * st.elem_bytes * st.sizes[0] * st.sizes[1] * st.sizes[2] for st, _ in specs) / 1e9:.1f} GB of grids"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_source": peak_kind},
-            "gpu_launches": uhs.launch_count() - n0, "clocks": clk}
+            "gpu_launches": launches, "clocks": clk}
     if errors:
         line["error_vs_oracle"] = errors
     if tuning:

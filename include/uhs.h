@@ -213,14 +213,18 @@ int uhs_error_norms_noalloc(const uhs_stencil_desc *desc, const uhs_memref *x, c
  * listed costliest first, and the launch's CTAs take them through an atomic
  * counter.  Each item is swept by its grid's variant (star/box, radius 1-3,
  * rank 2/3, FP64 in float pairs or native, FP32; boxes term by term, not as
- * separable passes).  uhs_batch_create plans the batch, uploads the per-grid
- * arguments, and captures the whole timestep loop (max T launches; a
- * program stops after its own T) into a CUDA graph; uhs_batch_run replays
- * it on any stream and reports through the batch's own status word.
+ * separable passes).  Grids of 2^21 interior points or more run instead as
+ * their own sweep launches with their standalone plan (tuner database or
+ * default tile, separable passes for rank-1 boxes), in up to four parallel
+ * branches of the same graph, concurrent with the persistent kernel.
+ * uhs_batch_create plans the batch, uploads the per-grid arguments, and
+ * captures the whole timestep loop (max T launches; a program stops after
+ * its own T) and the large grids' sweeps into one CUDA graph; uhs_batch_run
+ * replays it on any stream and reports through the batch's own status word.
  * Programs the streaming kernels do not cover (generic shapes,
  * UHS_ARITH_EXACT) are rejected with UHS_EUNSUPPORTED.  The grids must stay
  * allocated for the batch's lifetime.  params (may be NULL) applies to every
- * program; only its arith field is used. */
+ * program; the persistent kernel uses only its arith field. */
 typedef struct uhs_batch uhs_batch;
 
 int uhs_batch_create(const uhs_stencil_desc *descs, const uhs_memref *a, const uhs_memref *b, int32_t n,
@@ -228,7 +232,8 @@ int uhs_batch_create(const uhs_stencil_desc *descs, const uhs_memref *a, const u
 /* Replay the captured timestep loop on stream; synchronous unless flags has
  * UHS_FLAG_NO_SYNC. */
 int uhs_batch_run(uhs_batch *batch, void *stream, int32_t flags);
-/* Launches per replay, timesteps, work items per timestep (first step). */
+/* Launches per replay (persistent and large-grid sweeps), timesteps (max
+ * T), persistent-kernel work items in the first timestep. */
 int uhs_batch_stats(const uhs_batch *batch, int64_t *launches, int64_t *steps, int64_t *items);
 void uhs_batch_destroy(uhs_batch *batch);
 /* create + run + destroy */

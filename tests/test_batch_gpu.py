@@ -93,3 +93,26 @@ def test_batch_rejects_programs_outside_the_streaming_kernels(cuda):
     with pytest.raises(uhs.UhsError):
         uhs.Batch([st, st.with_(terms=[(0, 0, 0, 1.0)])], [a, a.clone()], [a.clone(), a.clone()])
     del odd
+
+
+def test_large_grids_run_as_their_own_launches_beside_the_persistent_kernel(cuda):
+    """Grids of 2^21 points or more are swept by their standalone plan in
+    parallel branches of the batch's graph: a float-pair 7-point star and an
+    FP32 2D 49-point box above the threshold (T = 1 and T = 4), with small
+    grids of several shapes in the persistent kernel; every grid matches its
+    oracle run, and the launch count adds the large grids' sweeps."""
+    small = cfg5_specs(n_grids=6, T=4, seed=17, side2=(40, 120), side3=(12, 30))
+    big1, _ = random_case(3, 1, "star", (136, 128, 128), 1, 31)
+    big2, _ = random_case(2, 3, "box", (1500, 1400), 4, 32, dtype=uhs.UHS_F32)
+    assert big1.interior_points >= 1 << 21 and big2.interior_points >= 1 << 21
+    specs = small + [(big1, 301), (big2, 302)]
+    a, b, host = _grids(specs)
+    batch = uhs.Batch([s for s, _ in specs], a, b)
+    stats = batch.stats()
+    assert stats["steps"] == 4
+    assert stats["launches"] == 4 + 1 + 4  # persistent steps + the large grids' sweeps
+    n0 = uhs.launch_count()
+    batch.run()
+    assert uhs.launch_count() - n0 == stats["launches"]
+    _check(specs, a, b, host)
+    batch.close()

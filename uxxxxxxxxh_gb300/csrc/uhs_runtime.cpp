@@ -596,7 +596,7 @@ static bool range_ok(const SweepSpec &sp, const GridView &a, const GridView &b, 
 }
 
 static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in, const GridView &out,
-                        cudaStream_t st) {
+                        cudaStream_t st, unsigned *err_word = nullptr) {
     if (pl.kernel == UHS_KERNEL_GENERIC) {
         cudaError_t e = launch_generic(sp, pl.cfg, in, out, st);
         if (e != cudaSuccess) return cuda_error(e, "generic sweep launch");
@@ -643,7 +643,7 @@ static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in,
     c.stream = st;
     int dev = 0;
     cudaGetDevice(&dev);
-    c.err = stream_error_word(dev, st);
+    c.err = err_word ? err_word : stream_error_word(dev, st);
     if (!c.err) return set_error(UHS_ENOMEM, "device error word allocation failed");
     const int eb = sp.dtype == UHS_F32 ? 4 : 8;
     CUtensorMap tmap;
@@ -885,9 +885,29 @@ static double batch_item_cost(int bx, int by, int zc, int nterms, int st, int ar
     return static_cast<double>(bx) * by * zc * (20.0 + per_term * nterms);
 }
 
+// Grids of at least kSoloPoints interior points run in a batch as their own
+// sweep launches -- the standalone plan: tuner-database or default tile,
+// separable passes for rank-1 boxes -- in up to kSoloBranches parallel
+// branches of the batch's graph, beside the persistent kernel that takes the
+// smaller grids.  On the 64-grid mixed suite (2D sides 256-8192, 3D 64-512)
+// that runs 42 grids solo; the persistent kernel alone took 188 ms, the
+// grids launched one after another 163 ms, and four concurrent streams 146 ms.
+constexpr int64_t kSoloPoints = int64_t(1) << 21;
+constexpr int kSoloBranches = 4;
+struct BatchSolo {
+    SweepSpec sp;
+    Plan pl;
+    GridView va, vb;
+    int T;
+    double work;  // points x T x (overhead + terms): the branch balance
+};
+
+static const uhs_params *effective_params(const uhs_stencil_desc *d, const uhs_params *p, uhs_params *buf);
+
 struct uhs_batch_impl {
     int dev = 0;
     int n = 0;
+    int n_solo = 0;
     int steps = 0;
     int64_t launches = 0, items0 = 0;
     BatchGrid *d_grids = nullptr;
@@ -919,6 +939,7 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
     B->n = n;
     std::vector<BatchGrid> host(static_cast<size_t>(n));
     std::vector<BatchGridHost> info(static_cast<size_t>(n));
+    std::vector<BatchSolo> solo;
     std::vector<std::vector<int4>> items(kNumPacks);
     {
         void *q = nullptr;
@@ -941,6 +962,33 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
         SweepSpec sp;
         make_spec(&descs[i], &sp);
         Plan pl;
+        const int64_t points = (sp.ub[0] - sp.lb[0]) * (sp.ub[1] - sp.lb[1]) * (sp.ub[2] - sp.lb[2]);
+        if (points >= kSoloPoints) {
+            uhs_params tuned, sparams;
+            const uhs_params *ep = effective_params(&descs[i], params, &tuned);
+            if (ep) sparams = *ep;
+            else uhs_params_default(&sparams);
+            sparams.k_temporal = 0;  // one step per launch
+            if ((rc = plan_sweep(sp, &sparams, va, &pl)) || pl.kernel != UHS_KERNEL_STREAM) {
+                // a tuned entry for another kernel family: the caller's own parameters
+                if (params) sparams = *params;
+                else uhs_params_default(&sparams);
+                sparams.k_temporal = 0;
+                if ((rc = plan_sweep(sp, &sparams, va, &pl))) return set_error(rc, "program %d: %s", i, uhs_last_error());
+            }
+            if (pl.kernel != UHS_KERNEL_STREAM)
+                return set_error(UHS_EUNSUPPORTED, "program %d is not a star/box stencil the batched kernel covers", i);
+            if (pl.auto_df32 && descs[i].iterations > 0 && !range_ok(sp, va, vb, descs[i].iterations, scan_stream)) {
+                pl.ar = kArNative;
+                pl.cfg.arith = UHS_ARITH_FMA;
+            }
+            const int nt = pl.factored ? 3 * (2 * pl.R + 1) : sp.nterms;
+            const double per_term = pl.st == kStF32 ? 1.0 : pl.ar == kArDf32 ? 6.0 : 14.0;
+            solo.push_back(BatchSolo{sp, pl, va, vb, descs[i].iterations,
+                                     static_cast<double>(points) * descs[i].iterations * (20.0 + per_term * nt)});
+            info[i] = BatchGridHost{-1, 0, 0, i, 1, 1, 1, 0, 0.0};
+            continue;
+        }
         uhs_params bp;
         if (params) bp = *params;
         else uhs_params_default(&bp);
@@ -996,6 +1044,7 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
     {
         double work = 0.0;
         for (int i = 0; i < n; ++i) {
+            if (info[i].pack < 0) continue;  // solo grid
             const BatchArgs &a0 = host[i].dir[0];
             work += info[i].item_cost * static_cast<double>((a0.ub2 - a0.lb2) * (a0.ub1 - a0.lb1)) /
                     (static_cast<double>(info[i].bx) * info[i].by) * static_cast<double>(a0.ub0 - a0.lb0);
@@ -1003,6 +1052,7 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
         const double target = work / (4.0 * device_sms() * 3);
         for (int i = 0; i < n; ++i) {
             BatchGridHost &g = info[i];
+            if (g.pack < 0) continue;
             int zc = g.zc;
             while (zc > 8 && g.item_cost * zc > target) zc /= 2;
             g.zc = zc;
@@ -1030,6 +1080,7 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
     for (int p = 0; p < kNumPacks; ++p) prefix[p].assign(static_cast<size_t>(steps), 0);
     for (int i : order) {
         const int p = info[i].pack;
+        if (p < 0) continue;
         const int bx = info[i].bx, by = info[i].by, zc = info[i].zc;
         const BatchArgs &a0 = host[i].dir[0];
         const int64_t tx = (a0.ub2 - a0.lb2 + bx - 1) / bx, ty = (a0.ub1 - a0.lb1 + by - 1) / by,
@@ -1077,18 +1128,74 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
             return set_error(UHS_ENOMEM, "batch item counters: allocation failed");
         B->d_counters = static_cast<int *>(q);
     }
-    // Capture the timestep loop.
-    if (steps > 0) {
+    // Solo grids: costliest first onto the least-loaded of up to
+    // kSoloBranches branches.
+    const int nbr = std::min<int>(kSoloBranches, static_cast<int>(solo.size()));
+    std::vector<std::vector<int>> branch(static_cast<size_t>(nbr));
+    {
+        std::vector<int> so(solo.size());
+        for (size_t k = 0; k < solo.size(); ++k) so[k] = static_cast<int>(k);
+        std::stable_sort(so.begin(), so.end(), [&](int x, int y) { return solo[x].work > solo[y].work; });
+        std::vector<double> load(static_cast<size_t>(nbr), 0.0);
+        for (int k : so) {
+            const int bi = static_cast<int>(std::min_element(load.begin(), load.end()) - load.begin());
+            branch[bi].push_back(k);
+            load[bi] += solo[k].work;
+        }
+    }
+    B->n_solo = static_cast<int>(solo.size());
+    for (const BatchSolo &g : solo) B->steps = std::max(B->steps, g.T);
+    // Capture the timestep loop of the persistent kernel and the solo grids'
+    // sweeps (forked branches joined back at the end).
+    if (steps > 0 || !solo.empty()) {
         cudaStream_t cs;
         if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
             return set_error(UHS_ECUDA, "capture stream creation failed");
         StreamGuard cg{cs};
+        std::vector<cudaStream_t> bs_(static_cast<size_t>(nbr), nullptr);
+        std::vector<cudaEvent_t> evs(static_cast<size_t>(nbr) + 1, nullptr);
+        struct BranchGuard {
+            std::vector<cudaStream_t> &s;
+            std::vector<cudaEvent_t> &e;
+            ~BranchGuard() {
+                for (auto x : s)
+                    if (x) cudaStreamDestroy(x);
+                for (auto x : e)
+                    if (x) cudaEventDestroy(x);
+            }
+        } bg{bs_, evs};
+        for (int k = 0; k < nbr; ++k)
+            if (cudaStreamCreateWithFlags(&bs_[k], cudaStreamNonBlocking) != cudaSuccess)
+                return set_error(UHS_ECUDA, "branch stream creation failed");
+        for (auto &ev : evs)
+            if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess)
+                return set_error(UHS_ECUDA, "branch event creation failed");
         if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
             return set_error(UHS_ECUDA, "graph capture could not start");
-        // every replay starts by zeroing the item counters (a memset node)
-        cudaError_t e = cudaMemsetAsync(B->d_counters, 0, sizeof(int) * n_counters, cs);
+        cudaError_t e = cudaSuccess;
+        int rc = UHS_OK;
         int64_t launches = 0;
-        for (int s = 0; s < steps && e == cudaSuccess; ++s) {
+        if (nbr > 0) {
+            e = cudaEventRecord(evs[nbr], cs);
+            for (int k = 0; k < nbr && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(bs_[k], evs[nbr], 0);
+            for (int k = 0; k < nbr && e == cudaSuccess && rc == UHS_OK; ++k) {
+                for (int gi : branch[k]) {
+                    const BatchSolo &g = solo[gi];
+                    for (int t = 0; t < g.T && rc == UHS_OK; ++t) {
+                        // T = 1: a -> b; even T: pairs a -> b, b -> a (as uhs_run)
+                        const bool fwd = (t % 2) == 0;
+                        rc = launch_sweep(g.sp, g.pl, fwd ? g.va : g.vb, fwd ? g.vb : g.va, bs_[k], err);
+                        ++launches;
+                    }
+                    if (rc) break;
+                }
+                if (rc == UHS_OK) e = cudaEventRecord(evs[k], bs_[k]);
+            }
+        }
+        // every replay zeroes the persistent kernel's item counters (a memset node)
+        if (e == cudaSuccess && rc == UHS_OK && n_counters > 0)
+            e = cudaMemsetAsync(B->d_counters, 0, sizeof(int) * n_counters, cs);
+        for (int s = 0; s < steps && e == cudaSuccess && rc == UHS_OK; ++s) {
             for (int p = 0; p < kNumPacks && e == cudaSuccess; ++p) {
                 const int64_t m = prefix[p][s];
                 if (m <= 0) continue;
@@ -1097,10 +1204,12 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
                 ++launches;
             }
         }
+        for (int k = 0; k < nbr && e == cudaSuccess && rc == UHS_OK; ++k) e = cudaStreamWaitEvent(cs, evs[k], 0);
         cudaGraph_t g = nullptr;
         const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
-        if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (rc != UHS_OK || e != cudaSuccess || e2 != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
+            if (rc != UHS_OK) return rc;
             return cuda_error(e != cudaSuccess ? e : e2, "batch graph capture");
         }
         B->graph = g;
