@@ -104,8 +104,10 @@ typedef struct uhs_stencil_desc {
 /* ---- tuning parameters ------------------------------------------------- */
 /* The launch parameters UHStencil fixes at compile time through pass options
  * (tile_sizes_l0/l1, inner_tile, use smem: include/Conversion/UHAffineToParallel/
- * Passes.td:6-101) become run-time values.  Zero means "let the backend choose"
- * (its tuner database, then the learned cost model, then defaults). */
+ * Passes.td:6-101) become run-time values.  Zero means "let the backend choose":
+ * the tuner database entry for the program when there is one (filled by the
+ * exhaustive tuner or by the learned cost model's picks, uhs_tune_put), else
+ * the planner's defaults, which are set per sweep class from GB300 timings. */
 enum {
     UHS_KERNEL_AUTO = 0,
     UHS_KERNEL_GENERIC = 1, /* any term list, smem plane ring, expression order */
@@ -118,7 +120,9 @@ typedef struct uhs_params {
     int32_t arith;        /* UHS_ARITH_* */
     int32_t tile_x;       /* CTA tile along x (fastest axis) */
     int32_t tile_y;       /* CTA tile along y (rank 3) */
-    int32_t tile_z;       /* planes streamed per CTA along the slowest axis */
+    int32_t tile_z;       /* planes (rows, rank 2) streamed per CTA along the slowest axis;
+                             0: about four waves of CTAs, at least 8 planes / 32 rows, capped
+                             for some sweep classes */
     int32_t k_temporal;   /* timesteps fused per pass over HBM */
     int32_t use_tma;      /* -1 off (cp.async loads), 0 auto, 1 on */
     int32_t flags;        /* UHS_FLAG_* */
