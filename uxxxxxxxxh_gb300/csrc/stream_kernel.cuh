@@ -395,11 +395,13 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
     unsigned phase = 0;  // mbarrier phase of plane j's slot
     int s_iss = PD % NSTG;
     int s_cmp = 0;  // compute-ring slot of plane j
-    // Radius-1 stars: three copies of the plane step, the length of the
-    // z-queue, so its shifts become register renaming (GB300: 3d7pt float
-    // pairs 175.4 -> 179.8 GStencil/s, 2d5pt 176.4 -> 182.3, FP32 490 -> 511
-    // in 2D).  Longer queues gain nothing and raise register use.
-    constexpr int UNROLL_Q = (STAR && R == 1) ? 3 : 1;
+    // Stars: 2R+1 copies of the plane step, the length of the z-queue, so its
+    // shifts become register renaming.  GB300, GStencil/s: 3d7pt float pairs
+    // 175.4 -> 179.8, 2d5pt 176.4 -> 182.3 (FP32 490 -> 511); at 8192^2
+    // 2d9pt 145.6 -> 153.8 (FP32 544 -> 587), 2d13pt 110.3 -> 124.5 (FP32
+    // 479 -> 521).  3D stars of radius 2-3, whose loop bodies are several
+    // times larger, lose (3d13pt 118.5 -> 94.4).
+    constexpr int UNROLL_Q = (STAR && (R == 1 || IS2D)) ? 2 * R + 1 : 1;
 #pragma unroll UNROLL_Q
     for (int j = 0; j < nq; ++j) {
         bool ok = true;
