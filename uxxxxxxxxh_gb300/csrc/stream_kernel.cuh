@@ -395,13 +395,15 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
     unsigned phase = 0;  // mbarrier phase of plane j's slot
     int s_iss = PD % NSTG;
     int s_cmp = 0;  // compute-ring slot of plane j
-    // Stars: 2R+1 copies of the plane step, the length of the z-queue, so its
-    // shifts become register renaming.  GB300, GStencil/s: 3d7pt float pairs
-    // 175.4 -> 179.8, 2d5pt 176.4 -> 182.3 (FP32 490 -> 511); at 8192^2
-    // 2d9pt 145.6 -> 153.8 (FP32 544 -> 587), 2d13pt 110.3 -> 124.5 (FP32
-    // 479 -> 521).  3D stars of radius 2-3, whose loop bodies are several
-    // times larger, lose (3d13pt 118.5 -> 94.4).
-    constexpr int UNROLL_Q = (STAR && (R == 1 || IS2D)) ? 2 * R + 1 : 1;
+    // 2R+1 copies of the plane step, the length of the z-queue, so its shifts
+    // become register renaming: 2D stars and separable boxes, and 3D radius-1
+    // stars.  GB300, GStencil/s: 3d7pt float pairs 175.4 -> 179.8, 2d5pt
+    // 176.4 -> 182.3 (FP32 490 -> 511); at 8192^2 2d9pt 145.6 -> 153.8 (FP32
+    // 544 -> 587), 2d13pt 110.3 -> 124.5 (FP32 479 -> 521), separable 2D
+    // boxes r1/r2/r3 +4/+14/+8 %.  3D stars of radius 2-3, whose loop bodies
+    // are several times larger, lose (3d13pt 118.5 -> 94.4), and so does the
+    // separable 3D r1 box (148.0 -> 145.6).
+    constexpr int UNROLL_Q = ((STAR && R == 1) || ((STAR || SEP) && IS2D)) ? 2 * R + 1 : 1;
 #pragma unroll UNROLL_Q
     for (int j = 0; j < nq; ++j) {
         bool ok = true;
