@@ -127,7 +127,10 @@ typedef struct uhs_params {
     int32_t use_tma;      /* -1 off (cp.async loads), 0 auto, 1 on */
     int32_t flags;        /* UHS_FLAG_* */
     int32_t vy;           /* points per thread along y (streaming kernel, rank 3) */
-    int32_t prefetch;     /* planes loaded ahead of the plane being computed */
+    int32_t prefetch;     /* planes (rows) loaded ahead of the one computed: fixed per kernel
+                             variant (streaming: 3 planes, 2 for radius 2-3 boxes swept term
+                             by term and for temporal fusion, 4 rows in 2D; generic: 1).
+                             0 or the built depth; uhs_plan reports it */
     int32_t factored;     /* set by uhs_plan: 1 when a separable box runs as 1D passes */
     int32_t reserved;
 } uhs_params;

@@ -79,3 +79,20 @@ def test_caller_tiles_override_the_defaults():
     p = plan(st, memref_raw(1 << 20, st.sizes),
              params=RunParams(tile_x=32, tile_y=32, vy=4, tile_z=24, flags=F.UHS_FLAG_NO_TUNE_DB))
     assert (p.tile_x, p.tile_y, p.vy, p.tile_z) == (32, 32, 4, 24)
+
+
+def test_prefetch_is_the_built_depth():
+    """Load-ahead depth is built into each variant: the plan reports it, a
+    caller may repeat it, any other value is refused."""
+    st, _ = random_case(3, 1, "star", (32, 32, 32), 2, 8)
+    assert plan(st, params=NO_DB).prefetch == 3
+    assert plan(st, params=RunParams(prefetch=3, flags=F.UHS_FLAG_NO_TUNE_DB)).prefetch == 3
+    with pytest.raises(_lib.UhsError) as ei:
+        plan(st, params=RunParams(prefetch=2, flags=F.UHS_FLAG_NO_TUNE_DB))
+    assert ei.value.code == F.UHS_EUNSUPPORTED
+    big_box, _ = random_case(3, 3, "box", (32, 32, 32), 2, 9)
+    assert plan(big_box, params=NO_DB).prefetch == 2
+    strip, _ = random_case(2, 2, "star", (64, 64), 2, 10)
+    assert plan(strip, params=NO_DB).prefetch == 4
+    with pytest.raises(_lib.UhsError):
+        plan(st, params=RunParams(kernel=F.UHS_KERNEL_GENERIC, prefetch=3, flags=F.UHS_FLAG_NO_TUNE_DB))

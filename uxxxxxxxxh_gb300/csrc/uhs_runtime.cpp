@@ -202,6 +202,7 @@ struct Plan {
     // streaming kernel
     int shape = -1, R = 0, st = 0, ar = 0, ld = kLdCpAsync, tile = 0, zchunk = 0;
     int zcap = 0;              // default launches: upper bound on the automatic z-chunk (0: none)
+    int pd = 0;                // planes (rows) the streaming kernel loads ahead: built into its variant
     std::vector<double> coef;  // coef_slot order
     bool auto_df32 = false;    // df32 chosen by UHS_ARITH_AUTO, subject to range_ok()
     bool factored = false;     // separable box run as 1D passes
@@ -371,6 +372,8 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
             return set_error(UHS_EINVAL, "tensor-core tiles are 16 columns wide (32 for radius 2), got %d", xt);
         if (view.s[0] >= (int64_t(1) << 31) || view.n[0] >= (int64_t(1) << 31))
             return set_error(UHS_EUNSUPPORTED, "planes of 2^31 elements or more need the generic kernel");
+        if (p->prefetch != 0)
+            return set_error(UHS_EUNSUPPORTED, "the tensor-core kernel's load-ahead is fixed (prefetch must be 0)");
         pl->kernel = cfg.kernel = UHS_KERNEL_MMA;
         cfg.tile_x = xt;
         cfg.tile_y = 128;
@@ -397,6 +400,8 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
         const int tx = cfg.tile_x > 0 ? cfg.tile_x : 32, ty = cfg.tile_y > 0 ? cfg.tile_y : 8;
         if (tx * ty > 256) return set_error(UHS_EINVAL, "tile %d x %d exceeds 256 threads", tx, ty);
         if (tx % 32 != 0) return set_error(UHS_EINVAL, "tile_x must be a multiple of 32 (got %d)", tx);
+        if (p->prefetch != 0 && p->prefetch != 1)
+            return set_error(UHS_EUNSUPPORTED, "the generic kernel loads one plane ahead (prefetch 0 or 1)");
         pl->kernel = kernel;
         cfg.kernel = kernel;
         return UHS_OK;
@@ -456,6 +461,13 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
         }
     }
     pl->tile = tile;
+    // Load-ahead depth: built into each variant (2D strips 4 rows; 3D 3
+    // planes, 2 for radius 2-3 boxes swept term by term; temporal fusion 2).
+    // A caller may state it, not choose another.
+    pl->pd = is2d ? 4 : cfg.k_temporal > 1 ? 2 : (shape == kBox3 && R >= 2 && !sep) ? 2 : 3;
+    if (p->prefetch != 0 && p->prefetch != pl->pd)
+        return set_error(UHS_EUNSUPPORTED, "this streaming variant loads %d %s ahead (prefetch %d)", pl->pd,
+                         is2d ? "rows" : "planes", p->prefetch);
     // Upper bound on the automatic z-chunk (about four waves of CTAs) for 3D
     // sweeps: shorter chunks measured faster in these classes (FP32 3d1r
     // star 632 vs 596 GStencil/s at 16 planes; float-pair 3d3r box 6.8 vs
@@ -1429,6 +1441,7 @@ int uhs_plan(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_params *p
         out->vy = sp.rank == 3 ? tile_shape(false, (pl.shape == kBox3 && pl.R >= 2) ? 3 : pl.tile).vy : 1;
         out->use_tma = pl.ld == kLdTma ? 1 : -1;
         out->factored = pl.factored ? 1 : 0;
+        out->prefetch = pl.pd;
     } else {
         out->tile_x = pl.cfg.tile_x > 0 ? pl.cfg.tile_x : 32;
         out->tile_y = pl.cfg.tile_y > 0 ? pl.cfg.tile_y : 8;
