@@ -96,3 +96,6 @@ def test_prefetch_is_the_built_depth():
     assert plan(strip, params=NO_DB).prefetch == 4
     with pytest.raises(_lib.UhsError):
         plan(st, params=RunParams(kernel=F.UHS_KERNEL_GENERIC, prefetch=3, flags=F.UHS_FLAG_NO_TUNE_DB))
+    with pytest.raises(_lib.UhsError):
+        plan(st, params=RunParams(kernel=F.UHS_KERNEL_GENERIC, use_tma=1, flags=F.UHS_FLAG_NO_TUNE_DB))
+    assert plan(st, params=RunParams(kernel=F.UHS_KERNEL_GENERIC, flags=F.UHS_FLAG_NO_TUNE_DB)).use_tma == -1

@@ -374,6 +374,7 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
             return set_error(UHS_EUNSUPPORTED, "planes of 2^31 elements or more need the generic kernel");
         if (p->prefetch != 0)
             return set_error(UHS_EUNSUPPORTED, "the tensor-core kernel's load-ahead is fixed (prefetch must be 0)");
+        if (cfg.use_tma > 0) return set_error(UHS_EUNSUPPORTED, "the tensor-core kernel stages planes without TMA");
         pl->kernel = cfg.kernel = UHS_KERNEL_MMA;
         cfg.tile_x = xt;
         cfg.tile_y = 128;
@@ -402,6 +403,7 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
         if (tx % 32 != 0) return set_error(UHS_EINVAL, "tile_x must be a multiple of 32 (got %d)", tx);
         if (p->prefetch != 0 && p->prefetch != 1)
             return set_error(UHS_EUNSUPPORTED, "the generic kernel loads one plane ahead (prefetch 0 or 1)");
+        if (cfg.use_tma > 0) return set_error(UHS_EUNSUPPORTED, "the generic kernel loads by cp.async, not TMA");
         pl->kernel = kernel;
         cfg.kernel = kernel;
         return UHS_OK;
