@@ -94,8 +94,10 @@ def test_prefetch_is_the_built_depth():
     assert plan(big_box, params=NO_DB).prefetch == 2
     strip, _ = random_case(2, 2, "star", (64, 64), 2, 10)
     assert plan(strip, params=NO_DB).prefetch == 4
-    with pytest.raises(_lib.UhsError):
-        plan(st, params=RunParams(kernel=F.UHS_KERNEL_GENERIC, prefetch=3, flags=F.UHS_FLAG_NO_TUNE_DB))
-    with pytest.raises(_lib.UhsError):
-        plan(st, params=RunParams(kernel=F.UHS_KERNEL_GENERIC, use_tma=1, flags=F.UHS_FLAG_NO_TUNE_DB))
-    assert plan(st, params=RunParams(kernel=F.UHS_KERNEL_GENERIC, flags=F.UHS_FLAG_NO_TUNE_DB)).use_tma == -1
+    gen = dict(kernel=F.UHS_KERNEL_GENERIC, arith=F.UHS_ARITH_FMA, flags=F.UHS_FLAG_NO_TUNE_DB)
+    assert plan(st, params=RunParams(**gen)).use_tma == -1
+    assert plan(st, params=RunParams(prefetch=1, **gen)).kernel == F.UHS_KERNEL_GENERIC
+    for bad in (dict(prefetch=3), dict(use_tma=1)):
+        with pytest.raises(_lib.UhsError) as ei:
+            plan(st, params=RunParams(**bad, **gen))
+        assert ei.value.code == F.UHS_EUNSUPPORTED
