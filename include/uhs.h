@@ -139,8 +139,10 @@ enum {
     UHS_FLAG_NO_SYNC = 1,    /* return without synchronising the stream */
     UHS_FLAG_NO_TUNE_DB = 2, /* ignore the tuner database for this call */
     UHS_FLAG_NO_FACTOR = 4,  /* sweep a separable box term by term, not as 1D passes */
-    UHS_FLAG_MMA_TMEM_A = 8  /* tensor-core path: stage the A operand in tensor memory
+    UHS_FLAG_MMA_TMEM_A = 8, /* tensor-core path: stage the A operand in tensor memory
                                 (tcgen05.cp) instead of reading it from shared memory */
+    UHS_FLAG_IN_PLACE = 16   /* FP64 grids in float pairs: sweep the FP64 grids themselves,
+                                not pair-resident copies (no scratch; see uhs_run) */
 };
 
 /* ---- entry points ------------------------------------------------------ */
@@ -164,7 +166,18 @@ int uhs_validate(const uhs_stencil_desc *desc, const uhs_memref *a, const uhs_me
  * a and b are device grids of identical shape; cells outside the domain are
  * read, never written, in both.  stream is a cudaStream_t (NULL = legacy
  * default stream).  Unless UHS_FLAG_NO_SYNC is set the call returns after the
- * stream has drained, which is what the reference's entry does. */
+ * stream has drained, which is what the reference's entry does.
+ *
+ * Pair-resident runs: FP64 grids swept in float-pair arithmetic (UHS_ARITH_AUTO
+ * after its range check, or UHS_ARITH_DF32) with T >= 8 sweeps run on
+ * float-pair copies of the grids.  Each value is split into its {hi, lo}
+ * floats once, the T sweeps read and write pairs, and the domain of both grids
+ * is joined back to FP64 at the end.  The halo is read from the FP64 grids and
+ * never written, so it stays bit-exact.  The copies (16 bytes per grid cell)
+ * are stream-ordered allocations from the device's default memory pool, which
+ * the library sets to keep freed memory for reuse (trim it with
+ * cudaMemPoolTrimTo).  When that allocation fails, or with UHS_FLAG_IN_PLACE,
+ * the sweeps run on the FP64 grids directly, splitting on every load. */
 int uhs_run(const uhs_stencil_desc *desc, const uhs_memref *a, const uhs_memref *b,
             const uhs_params *params, void *stream);
 

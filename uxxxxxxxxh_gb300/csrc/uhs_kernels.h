@@ -81,6 +81,14 @@ struct ErrNormsCall {
 };
 cudaError_t launch_error_norms(const ErrNormsCall &c);
 
+// Pair-resident runs (pairs.cu): an FP64 grid's values split into a
+// contiguous float-pair grid (the whole grid, or only the cells outside the
+// domain [lb, ub)), and the domain of a float-pair grid joined back.
+cudaError_t launch_to_pairs(const GridView &src, const GridView &dst, const int64_t lb[3], const int64_t ub[3],
+                            bool halo_only, unsigned *err, cudaStream_t st);
+cudaError_t launch_from_pairs(const GridView &src, const GridView &dst, const int64_t lb[3], const int64_t ub[3],
+                              cudaStream_t st);
+
 // Max of the biased exponent fields of n_words doubles into *out (atomicMax;
 // *out must start at 0).
 cudaError_t launch_max_exponent(const void *data, int64_t n_words, unsigned *out, int sms, cudaStream_t st);

@@ -1314,6 +1314,78 @@ static const uhs_params *effective_params(const uhs_stencil_desc *d, const uhs_p
     buf->flags = p ? p->flags : 0;
     return buf;
 }
+// Stream-ordered scratch from the device's default memory pool, which is set
+// once per device to keep freed memory for reuse (later runs then allocate
+// without a device-wide synchronisation).  Honours the diagnostic cap.
+static cudaError_t dev_alloc_async(void **p, size_t bytes, cudaStream_t st) {
+    const int64_t cap = g_alloc_cap.load(std::memory_order_relaxed);
+    if (cap > 0 && static_cast<int64_t>(bytes) > cap) return cudaErrorMemoryAllocation;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    static std::mutex mu;
+    static bool kept[64] = {};
+    if (dev >= 0 && dev < 64) {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!kept[dev]) {
+            cudaMemPool_t pool;
+            if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+                uint64_t keep = UINT64_MAX;
+                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            }
+            kept[dev] = true;
+        }
+    }
+    const cudaError_t e = cudaMallocAsync(p, bytes, st);
+    if (e != cudaSuccess) cudaGetLastError();  // not sticky: the caller falls back
+    return e;
+}
+
+// Pair-resident run of a float-pair FP64 program (see uhs_run in uhs.h):
+// *ran stays false when the scratch could not be had or planned, and the
+// caller then sweeps the FP64 grids in place.
+constexpr int kPairMinT = 8;
+static int run_pair_resident(const SweepSpec &sp, const uhs_params *p, const GridView &va, const GridView &vb,
+                             int T, cudaStream_t st, bool *ran) {
+    *ran = false;
+    const int64_t n0 = va.n[0], n1 = va.n[1], n2 = va.n[2];
+    const size_t bytes = static_cast<size_t>(n0 * n1 * n2) * sizeof(double);
+    void *buf = nullptr;
+    if (dev_alloc_async(&buf, 2 * bytes, st) != cudaSuccess) return UHS_OK;
+    const GridView pa{buf, {n0, n1, n2}, {n1 * n2, n2, 1}};
+    const GridView pb{static_cast<char *>(buf) + bytes, {n0, n1, n2}, {n1 * n2, n2, 1}};
+    SweepSpec sp2 = sp;
+    sp2.dtype = UHS_F32X2;
+    uhs_params q;
+    if (p) q = *p;
+    else uhs_params_default(&q);
+    q.arith = UHS_ARITH_DF32;
+    Plan pl2;
+    if (plan_sweep(sp2, &q, pa, &pl2) != UHS_OK || pl2.kernel != UHS_KERNEL_STREAM) {
+        cudaFreeAsync(buf, st);
+        set_error(UHS_OK, "");
+        return UHS_OK;
+    }
+    *ran = true;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    unsigned *err = stream_error_word(dev, st);
+    int rc = UHS_OK;
+    cudaError_t e = launch_to_pairs(va, pa, sp.lb, sp.ub, false, err, st);
+    if (e == cudaSuccess) e = launch_to_pairs(vb, pb, sp.lb, sp.ub, true, err, st);
+    if (e != cudaSuccess) rc = cuda_error(e, "float-pair conversion");
+    for (int it = 0; it < T / 2 && rc == UHS_OK; ++it) {
+        if ((rc = launch_sweep(sp2, pl2, pa, pb, st))) break;
+        rc = launch_sweep(sp2, pl2, pb, pa, st);
+    }
+    if (rc == UHS_OK) {
+        e = launch_from_pairs(pa, va, sp.lb, sp.ub, st);
+        if (e == cudaSuccess) e = launch_from_pairs(pb, vb, sp.lb, sp.ub, st);
+        if (e != cudaSuccess) rc = cuda_error(e, "float-pair conversion");
+    }
+    cudaFreeAsync(buf, st);
+    return rc;
+}
+
 }  // namespace uhs
 
 using namespace uhs;
@@ -1505,6 +1577,12 @@ int uhs_run(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_memref *b,
             fwd = !fwd;
         }
         return finish(p, st);
+    }
+    if (pl.kernel == UHS_KERNEL_STREAM && pl.st == kStF64 && pl.ar == kArDf32 && d->iterations >= kPairMinT &&
+        !(p && (p->flags & UHS_FLAG_IN_PLACE))) {
+        bool ran = false;
+        rc = run_pair_resident(sp, p, va, vb, d->iterations, st, &ran);
+        if (ran) return rc ? rc : finish(p, st);
     }
     if (d->iterations == 1) {
         if ((rc = launch_sweep(sp, pl, va, vb, st))) return rc;
