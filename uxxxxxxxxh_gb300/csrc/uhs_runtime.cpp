@@ -1578,8 +1578,15 @@ int uhs_run(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_memref *b,
         }
         return finish(p, st);
     }
+    // Pair-resident where it measured faster on GB300: stars of radius 1-2
+    // (3d7pt 180 -> 268, 3d13pt 119 -> 182, 2d5pt 183 -> 269 GStencil/s) and
+    // separable boxes (cfg3's 343-point Gaussian 47.9 -> 51.2).  Radius-3 stars
+    // and boxes swept term by term gain too little per sweep to pay for the
+    // conversions at T = 10 (3d19pt 82.4 in place, 80.8 pair-resident; 3d27pt
+    // 79.7 / 75.2; 3d343pt 5.73 / 5.15).
+    const bool pair_shape = pl.factored || ((pl.shape == kStar3 || pl.shape == kStar2) && pl.R <= 2);
     if (pl.kernel == UHS_KERNEL_STREAM && pl.st == kStF64 && pl.ar == kArDf32 && d->iterations >= kPairMinT &&
-        !(p && (p->flags & UHS_FLAG_IN_PLACE))) {
+        pair_shape && !(p && (p->flags & UHS_FLAG_IN_PLACE))) {
         bool ran = false;
         rc = run_pair_resident(sp, p, va, vb, d->iterations, st, &ran);
         if (ran) return rc ? rc : finish(p, st);
