@@ -910,12 +910,32 @@ static double batch_item_cost(int bx, int by, int zc, int nterms, int st, int ar
 // two branches 147.5 ms, eight 144.3 ms.
 constexpr int64_t kSoloPoints = int64_t(1) << 21;
 constexpr int kSoloBranches = 4;
+// Float-pair FP64 programs that run pair-resident (uhs_run in uhs.h; the
+// batches' solo grids): T >= kPairMinT sweeps of a star of radius 1-2 or a
+// separable box, where that measured faster on GB300 (3d7pt 180 -> 268,
+// 3d13pt 119 -> 182, 2d5pt 183 -> 269 GStencil/s; cfg3's separable
+// 343-point Gaussian 47.9 -> 51.2).  Radius-3 stars and boxes swept term by
+// term gain too little per sweep to pay for the conversions at T = 10
+// (3d19pt 82.4 in place, 80.8 pair-resident; 3d27pt 79.7 / 75.2; 3d343pt
+// 5.73 / 5.15).
+constexpr int kPairMinT = 8;
+static bool pair_eligible(const Plan &pl, int T, const uhs_params *p) {
+    return pl.kernel == UHS_KERNEL_STREAM && pl.st == kStF64 && pl.ar == kArDf32 && T >= kPairMinT &&
+           (pl.factored || ((pl.shape == kStar3 || pl.shape == kStar2) && pl.R <= 2)) &&
+           !(p && (p->flags & UHS_FLAG_IN_PLACE));
+}
+
 struct BatchSolo {
     SweepSpec sp;
     Plan pl;
     GridView va, vb;
     int T;
     double work;  // points x T x (overhead + terms): the branch balance
+    // pair-resident: float-pair copies owned by the batch, and their plan
+    bool pairs = false;
+    SweepSpec sp2;
+    Plan pl2;
+    GridView pa{}, pb{};
 };
 
 static const uhs_params *effective_params(const uhs_stencil_desc *d, const uhs_params *p, uhs_params *buf);
@@ -930,6 +950,7 @@ struct uhs_batch_impl {
     int4 *d_items[kNumPacks] = {nullptr, nullptr};
     int *d_counters = nullptr;  // one item counter per (timestep, pack), zeroed at each replay
     unsigned *d_status = nullptr;  // the batch's own status word (its graph may replay on any stream)
+    std::vector<void *> scratch;   // float-pair copies of pair-resident solo grids
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -943,6 +964,7 @@ static void batch_free(uhs_batch_impl *b) {
     if (b->d_status) cudaFree(b->d_status);
     for (auto *p : b->d_items)
         if (p) cudaFree(p);
+    for (auto *p : b->scratch) cudaFree(p);
     delete b;
 }
 
@@ -1000,8 +1022,32 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
             }
             const int nt = pl.factored ? 3 * (2 * pl.R + 1) : sp.nterms;
             const double per_term = pl.st == kStF32 ? 1.0 : pl.ar == kArDf32 ? 6.0 : 14.0;
-            solo.push_back(BatchSolo{sp, pl, va, vb, descs[i].iterations,
-                                     static_cast<double>(points) * descs[i].iterations * (20.0 + per_term * nt)});
+            BatchSolo g;
+            g.sp = sp;
+            g.pl = pl;
+            g.va = va;
+            g.vb = vb;
+            g.T = descs[i].iterations;
+            g.work = static_cast<double>(points) * descs[i].iterations * (20.0 + per_term * nt);
+            if (pair_eligible(pl, g.T, &sparams)) {
+                const int64_t n0 = va.n[0], n1 = va.n[1], n2 = va.n[2];
+                const size_t bytes = static_cast<size_t>(n0 * n1 * n2) * sizeof(double);
+                void *buf = nullptr;
+                if (dev_alloc(&buf, 2 * bytes) == cudaSuccess) {
+                    B->scratch.push_back(buf);
+                    g.pa = GridView{buf, {n0, n1, n2}, {n1 * n2, n2, 1}};
+                    g.pb = GridView{static_cast<char *>(buf) + bytes, {n0, n1, n2}, {n1 * n2, n2, 1}};
+                    g.sp2 = sp;
+                    g.sp2.dtype = UHS_F32X2;
+                    uhs_params q = sparams;
+                    q.arith = UHS_ARITH_DF32;
+                    g.pairs = plan_sweep(g.sp2, &q, g.pa, &g.pl2) == UHS_OK && g.pl2.kernel == UHS_KERNEL_STREAM;
+                    if (!g.pairs) set_error(UHS_OK, "");
+                } else {
+                    cudaGetLastError();  // no copies: this grid sweeps in place
+                }
+            }
+            solo.push_back(g);
             info[i] = BatchGridHost{-1, 0, 0, i, 1, 1, 1, 0, 0.0};
             continue;
         }
@@ -1197,15 +1243,30 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
             for (int k = 0; k < nbr && e == cudaSuccess && rc == UHS_OK; ++k) {
                 for (int gi : branch[k]) {
                     const BatchSolo &g = solo[gi];
+                    if (g.pairs) {  // split a, and b's halo, into the copies
+                        e = launch_to_pairs(g.va, g.pa, g.sp.lb, g.sp.ub, false, err, bs_[k]);
+                        if (e == cudaSuccess) e = launch_to_pairs(g.vb, g.pb, g.sp.lb, g.sp.ub, true, err, bs_[k]);
+                        launches += 2;
+                        if (e != cudaSuccess) break;
+                    }
+                    const SweepSpec &ssp = g.pairs ? g.sp2 : g.sp;
+                    const Plan &spl = g.pairs ? g.pl2 : g.pl;
+                    const GridView &ga = g.pairs ? g.pa : g.va, &gb = g.pairs ? g.pb : g.vb;
                     for (int t = 0; t < g.T && rc == UHS_OK; ++t) {
                         // T = 1: a -> b; even T: pairs a -> b, b -> a (as uhs_run)
                         const bool fwd = (t % 2) == 0;
-                        rc = launch_sweep(g.sp, g.pl, fwd ? g.va : g.vb, fwd ? g.vb : g.va, bs_[k], err);
+                        rc = launch_sweep(ssp, spl, fwd ? ga : gb, fwd ? gb : ga, bs_[k], err);
                         ++launches;
                     }
                     if (rc) break;
+                    if (g.pairs) {  // both domains back (T >= 8 sweeps wrote both grids)
+                        e = launch_from_pairs(g.pa, g.va, g.sp.lb, g.sp.ub, bs_[k]);
+                        if (e == cudaSuccess) e = launch_from_pairs(g.pb, g.vb, g.sp.lb, g.sp.ub, bs_[k]);
+                        launches += 2;
+                        if (e != cudaSuccess) break;
+                    }
                 }
-                if (rc == UHS_OK) e = cudaEventRecord(evs[k], bs_[k]);
+                if (rc == UHS_OK && e == cudaSuccess) e = cudaEventRecord(evs[k], bs_[k]);
             }
         }
         // every replay zeroes the persistent kernel's item counters (a memset node)
@@ -1343,7 +1404,6 @@ static cudaError_t dev_alloc_async(void **p, size_t bytes, cudaStream_t st) {
 // Pair-resident run of a float-pair FP64 program (see uhs_run in uhs.h):
 // *ran stays false when the scratch could not be had or planned, and the
 // caller then sweeps the FP64 grids in place.
-constexpr int kPairMinT = 8;
 static int run_pair_resident(const SweepSpec &sp, const uhs_params *p, const GridView &va, const GridView &vb,
                              int T, cudaStream_t st, bool *ran) {
     *ran = false;
@@ -1578,15 +1638,7 @@ int uhs_run(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_memref *b,
         }
         return finish(p, st);
     }
-    // Pair-resident where it measured faster on GB300: stars of radius 1-2
-    // (3d7pt 180 -> 268, 3d13pt 119 -> 182, 2d5pt 183 -> 269 GStencil/s) and
-    // separable boxes (cfg3's 343-point Gaussian 47.9 -> 51.2).  Radius-3 stars
-    // and boxes swept term by term gain too little per sweep to pay for the
-    // conversions at T = 10 (3d19pt 82.4 in place, 80.8 pair-resident; 3d27pt
-    // 79.7 / 75.2; 3d343pt 5.73 / 5.15).
-    const bool pair_shape = pl.factored || ((pl.shape == kStar3 || pl.shape == kStar2) && pl.R <= 2);
-    if (pl.kernel == UHS_KERNEL_STREAM && pl.st == kStF64 && pl.ar == kArDf32 && d->iterations >= kPairMinT &&
-        pair_shape && !(p && (p->flags & UHS_FLAG_IN_PLACE))) {
+    if (pair_eligible(pl, d->iterations, p)) {
         bool ran = false;
         rc = run_pair_resident(sp, p, va, vb, d->iterations, st, &ran);
         if (ran) return rc ? rc : finish(p, st);
