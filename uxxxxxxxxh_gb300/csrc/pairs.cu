@@ -26,12 +26,14 @@ struct PairConv {
     unsigned *err;
 };
 
-// FP64 -> pairs over the whole grid, or its halo only: one CTA per row at a
-// time (rows of the grid, slowest axes flattened), threads striding along x.
+// FP64 -> pairs over the whole grid, or its halo only: one warp per row at a
+// time (rows of the grid, slowest axes flattened), lanes striding along x.
 __global__ void __launch_bounds__(kConvThreads) k_to_pairs(const PairConv a) {
     const int64_t rows = a.n0 * a.n1;
+    const int wpb = kConvThreads / 32, lane = threadIdx.x & 31;
     unsigned rerr = 0;
-    for (int64_t row = blockIdx.x; row < rows; row += gridDim.x) {
+    for (int64_t row = static_cast<int64_t>(blockIdx.x) * wpb + (threadIdx.x >> 5); row < rows;
+         row += static_cast<int64_t>(gridDim.x) * wpb) {
         const int64_t z = row / a.n1, y = row % a.n1;
         const double *s = static_cast<const double *>(a.src) + z * a.s0s + y * a.s1s;
         float2 *d = static_cast<float2 *>(a.dst) + z * a.s0d + y * a.s1d;
@@ -39,34 +41,41 @@ __global__ void __launch_bounds__(kConvThreads) k_to_pairs(const PairConv a) {
         if (a.halo_only && inner_row) {
             // the row's x halo only: [0, lb2) and [ub2, n2)
             const int64_t left = a.lb2, right = a.n2 - a.ub2;
-            for (int64_t i = threadIdx.x; i < left + right; i += blockDim.x) {
+            for (int64_t i = lane; i < left + right; i += 32) {
                 const int64_t x = i < left ? i : a.ub2 + (i - left);
                 d[x] = split_f64(s[x], rerr);
             }
         } else {
-            for (int64_t x = threadIdx.x; x < a.n2; x += blockDim.x) d[x] = split_f64(s[x], rerr);
+#pragma unroll 4
+            for (int64_t x = lane; x < a.n2; x += 32) d[x] = split_f64(s[x], rerr);
         }
     }
     if (rerr) atomicOr(a.err, kDevErrRange);
 }
 
-// pairs -> FP64 over the domain [lb, ub): each value the double nearest hi + lo.
+// pairs -> FP64 over the domain [lb, ub): each value the double nearest
+// hi + lo.  One warp per row at a time.
 __global__ void __launch_bounds__(kConvThreads) k_from_pairs(const PairConv a) {
     const int64_t ny = a.ub1 - a.lb1, rows = (a.ub0 - a.lb0) * ny;
-    for (int64_t row = blockIdx.x; row < rows; row += gridDim.x) {
+    const int wpb = kConvThreads / 32, lane = threadIdx.x & 31;
+    for (int64_t row = static_cast<int64_t>(blockIdx.x) * wpb + (threadIdx.x >> 5); row < rows;
+         row += static_cast<int64_t>(gridDim.x) * wpb) {
         const int64_t z = a.lb0 + row / ny, y = a.lb1 + row % ny;
         const float2 *s = static_cast<const float2 *>(a.src) + z * a.s0s + y * a.s1s;
         double *d = static_cast<double *>(a.dst) + z * a.s0d + y * a.s1d;
-        for (int64_t x = a.lb2 + threadIdx.x; x < a.ub2; x += blockDim.x) {
+#pragma unroll 4
+        for (int64_t x = a.lb2 + lane; x < a.ub2; x += 32) {
             const float2 v = s[x];
             d[x] = join_f64(v.x, v.y);
         }
     }
 }
 
+// CTAs of 8 warps, one row per warp at a time: at most 8 resident CTAs on
+// each of 152 SMs.
 unsigned conv_blocks(int64_t rows) {
-    const int64_t cap = int64_t(152) * 16;
-    return static_cast<unsigned>(rows < 1 ? 1 : rows < cap ? rows : cap);
+    const int64_t need = (rows + kConvThreads / 32 - 1) / (kConvThreads / 32), cap = int64_t(152) * 8;
+    return static_cast<unsigned>(need < 1 ? 1 : need < cap ? need : cap);
 }
 
 }  // namespace
