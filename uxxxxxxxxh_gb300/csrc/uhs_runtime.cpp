@@ -56,6 +56,14 @@ int set_error(int code, const char *fmt, ...) {
     return code;
 }
 
+// Keeps the thread's last-error message across an optional step whose
+// failure the caller works around (the message then still describes the last
+// call that failed).
+struct ErrorMessageGuard {
+    std::string saved = t_err;
+    ~ErrorMessageGuard() { t_err = saved; }
+};
+
 static int cuda_error(cudaError_t e, const char *what) {
     return set_error(UHS_ECUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
 }
@@ -1041,8 +1049,8 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
                     g.sp2.dtype = UHS_F32X2;
                     uhs_params q = sparams;
                     q.arith = UHS_ARITH_DF32;
+                    ErrorMessageGuard keep;
                     g.pairs = plan_sweep(g.sp2, &q, g.pa, &g.pl2) == UHS_OK && g.pl2.kernel == UHS_KERNEL_STREAM;
-                    if (!g.pairs) set_error(UHS_OK, "");
                 } else {
                     cudaGetLastError();  // no copies: this grid sweeps in place
                 }
@@ -1420,9 +1428,13 @@ static int run_pair_resident(const SweepSpec &sp, const uhs_params *p, const Gri
     else uhs_params_default(&q);
     q.arith = UHS_ARITH_DF32;
     Plan pl2;
-    if (plan_sweep(sp2, &q, pa, &pl2) != UHS_OK || pl2.kernel != UHS_KERNEL_STREAM) {
+    bool planned;
+    {
+        ErrorMessageGuard keep;
+        planned = plan_sweep(sp2, &q, pa, &pl2) == UHS_OK && pl2.kernel == UHS_KERNEL_STREAM;
+    }
+    if (!planned) {
         cudaFreeAsync(buf, st);
-        set_error(UHS_OK, "");
         return UHS_OK;
     }
     *ran = true;
