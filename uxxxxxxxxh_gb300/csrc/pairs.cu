@@ -1,7 +1,8 @@
 // FP64 grid <-> float-pair grid conversion for pair-resident runs.
 //
-// A program of T >= kPairMinT sweeps on FP64 grids in float-pair arithmetic
-// runs on float-pair copies of its grids: each FP64 value is split once
+// A program of T >= 8 float-pair sweeps on FP64 grids (a star of radius 1-2
+// or a separable box; pair_eligible in uhs_runtime.cpp) runs on float-pair
+// copies of its grids: each FP64 value is split once
 // (split_f64) into a {hi, lo} float pair, the T sweeps read and write pairs
 // (no split on every load, no join on every store: the sweep kernel's
 // float-pair variant), and the domain of each grid a sweep wrote is joined
