@@ -920,7 +920,7 @@ constexpr int64_t kSoloPoints = int64_t(1) << 21;
 constexpr int kSoloBranches = 4;
 // Float-pair FP64 programs that run pair-resident (uhs_run in uhs.h; the
 // batches' solo grids): T >= kPairMinT sweeps of a star of radius 1-2 or a
-// separable box, where that measured faster on GB300 (3d7pt 180 -> 268,
+// separable box, where that measured faster on GB300 (3d7pt 180 -> 278,
 // 3d13pt 119 -> 182, 2d5pt 183 -> 269 GStencil/s; cfg3's separable
 // 343-point Gaussian 47.9 -> 51.2).  Radius-3 stars and boxes swept term by
 // term gain too little per sweep to pay for the conversions at T = 10
