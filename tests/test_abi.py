@@ -127,3 +127,34 @@ def test_short_or_one_sided_reach_runs_on_the_generic_kernel():
     # a full star still plans on the streaming kernel
     st3 = st2.with_(terms=st2.terms + [(1, 0, 0, 0.0)], ub=(5, 9, 11))
     assert uhs.plan(st3).kernel == uhs.UHS_KERNEL_STREAM
+
+
+def _header_constants():
+    """Every UHS_* enumerator and numeric #define of include/uhs.h with its
+    value (enumerators without an initialiser count up from the previous)."""
+    text = open(os.path.join(ROOT, "include", "uhs.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    out = {}
+    for body in re.findall(r"enum\s*(?:\w+\s*)?(?::\s*\w+\s*)?\{(.*?)\}", text, flags=re.S):
+        value = -1
+        for item in body.split(","):
+            item = item.strip()
+            if not item:
+                continue
+            m = re.fullmatch(r"(UHS_\w+)\s*(?:=\s*(-?\w+))?", item)
+            assert m, item
+            value = int(m.group(2), 0) if m.group(2) is not None else value + 1
+            out[m.group(1)] = value
+    for name, val in re.findall(r"^#define\s+(UHS_\w+)\s+(-?\d+)\s*$", text, flags=re.M):
+        out[name] = int(val)
+    return out
+
+
+def test_python_constants_mirror_the_header():
+    consts = _header_constants()
+    assert {"UHS_OK", "UHS_F32X2", "UHS_ARITH_DF32", "UHS_KERNEL_MMA", "UHS_FLAG_IN_PLACE"} <= set(consts)
+    for name, value in consts.items():
+        if name == "UHS_ABI_VERSION":
+            continue
+        assert hasattr(_lib, name), f"_lib has no {name}"
+        assert getattr(_lib, name) == value, (name, getattr(_lib, name), value)
