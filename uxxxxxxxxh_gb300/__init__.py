@@ -6,6 +6,7 @@ kernels and the host runtime that replaces UHStencil's generated
 (descriptors, DSL reader, run/sweep calls); it holds no compute of its own.
 """
 from ._lib import (UHS_ARITH_AUTO, UHS_ARITH_DF32, UHS_ARITH_EXACT, UHS_ARITH_FMA, UHS_F32, UHS_F32X2, UHS_F64,
+                   UHS_FLAG_IN_PLACE, UHS_FLAG_MMA_TMEM_A, UHS_FLAG_NO_FACTOR, UHS_FLAG_NO_SYNC, UHS_FLAG_NO_TUNE_DB,
                    UHS_KERNEL_AUTO, UHS_KERNEL_GENERIC, UHS_KERNEL_MMA, UHS_KERNEL_STREAM, UhsError, lib)
 from .runtime import (Batch, RunParams, error_norms, launch_count, memref_of, memref_raw, plan, probe_wait_timeout, run,
                       sweep, validate)
@@ -14,6 +15,7 @@ from .stencil import (SHAPES, Stencil, box_offsets, make_stencil, offsets_for, p
 
 __all__ = [
     "UHS_ARITH_AUTO", "UHS_ARITH_DF32", "UHS_ARITH_EXACT", "UHS_ARITH_FMA", "UHS_F32", "UHS_F32X2", "UHS_F64",
+    "UHS_FLAG_IN_PLACE", "UHS_FLAG_MMA_TMEM_A", "UHS_FLAG_NO_FACTOR", "UHS_FLAG_NO_SYNC", "UHS_FLAG_NO_TUNE_DB",
     "UHS_KERNEL_AUTO", "UHS_KERNEL_GENERIC", "UHS_KERNEL_MMA", "UHS_KERNEL_STREAM", "UhsError", "lib",
     "Batch", "RunParams", "error_norms", "launch_count", "memref_of", "memref_raw", "plan", "probe_wait_timeout", "run",
     "sweep", "validate", "SHAPES",
