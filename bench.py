@@ -4,7 +4,8 @@ Workload (default): 3d1r_star (7-point) FP64 on a 512^3 interior with a
 1-cell zero halo, U[-1,1) data, 7 normalised U[0,1) coefficients, T = 50
 sweeps with double-buffer ping-pong -- the configuration the GStencil/s metric
 is quoted on.  One "step" is one complete program run (T sweeps of the grid)
-through uhs_run().
+through uhs_run() on the workload's input: both grids are reset to it before
+every step, outside the timed interval.
 
 Reported (one JSON line, rank 0):
   value      GStencil/s = interior points * T / time, grids resident in HBM
@@ -21,6 +22,10 @@ Reported (one JSON line, rank 0):
   fp32       the same workload on FP32 grids, with its L2 error against the
              FP64 oracle and, at full size on the GPU, against this library's
              FP64 sweep of the same rounded input (uhs.error_norms)
+  plain_f64  the same workload in native IEEE binary64 arithmetic (DFMA), its
+             kernel against the HBM roofline and the FP64 pipe's measured
+             DFMA rate; speedup_vs_plain_f64 sets the default FP64 path and
+             FP32 beside it, each with its error against the FP64 oracle
 Inputs (1.09 GB per grid) are larger than the 129 MB L2, so no flush is
 needed between timed iterations.
 
@@ -60,17 +65,43 @@ def parse_args():
     p.add_argument("--no-cpu", action="store_true", help="skip the oracle (profiling runs)")
     p.add_argument("--no-fp32", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-plain", action="store_true", help="skip the plain (native) FP64 arm")
     p.add_argument("--no-tune", action="store_true", help="cfg5: skip the standalone cost-model / exhaustive comparison")
     return p.parse_args()
 
 
-# DRAM bytes per point-update of the 7-point star sweep kernels, from one ncu
-# capture of each on GB300 (320^3 interior, dram__bytes_read.sum +
-# dram__bytes_write.sum of one launch over its 32.8 M points).  A launch's
-# traffic grows with the points it sweeps, so the per-launch figure for
-# another size is this times its interior points.
-NCU_BYTES_PER_POINT = {("star7", "f64", "df32"): 15.10, ("star7", "f64", "fma"): 15.20, ("star7", "f32", "fma"): 6.77,
-                       ("star7", "f32x2", "df32"): 15.00}
+# DRAM bytes per point-update of the sweep kernels, from one ncu capture of
+# each on GB300 (dram__bytes_read.sum + dram__bytes_write.sum of one launch
+# over its interior points; 320^3 interiors for rank 3, 8192^2 for rank 2,
+# profiles/ holds the summaries).  A launch's traffic grows with the points it
+# sweeps, so the per-launch figure for another size is this times its
+# interior points.  Keyed by (shape, grid element type the kernel sweeps,
+# arithmetic).
+NCU_BYTES_PER_POINT = {
+    ("3d1r_star", "f64", "df32"): 15.10, ("3d1r_star", "f64", "fma"): 15.20, ("3d1r_star", "f32", "fma"): 6.77,
+    ("3d1r_star", "f32x2", "df32"): 15.00,
+}
+
+
+def traffic_key(st, kernel_elem: str, arith: str, factored: bool):
+    star = all(sum(1 for v in t[:3] if v) <= 1 for t in st.terms)
+    kind = "star" if star else ("box_sep" if factored else "box")
+    return (f"{st.rank}d{max(st.radius)}r_{kind}", kernel_elem, arith)
+
+
+def workload_label(st) -> str:
+    """The workload's name as both arms print it in config.workload."""
+    return (f"{st.name}: {'x'.join(str(u - l) for l, u in zip(st.lb, st.ub))} interior, "
+            f"halo {st.lb[2]}, T={st.iterations}")
+
+
+ARITH_LABELS = {1: "fma (IEEE binary64 DFMA for FP64 grids, FFMA for FP32)",
+                2: "exact (separately rounded IEEE products and sums, expression order)",
+                3: "df32 (float pairs: 48-bit significand, FP32 exponent range, on the FP32 pipes)"}
+
+
+def arith_names_full(code: int) -> str:
+    return ARITH_LABELS.get(code, str(code))
 
 
 def load_peaks():
@@ -151,6 +182,7 @@ def cpu_sample(st, a0, budget_s: float = 12.0):
     whole-grid sweeps, as many as fit the time budget (at most T)."""
     import oracle
     a, b = a0.copy(), a0.copy()
+    oracle.set_threads(os.cpu_count() or 1)
     t0 = time.perf_counter()
     oracle.sweep_f64(st, a, b)
     t1 = time.perf_counter() - t0
@@ -164,9 +196,28 @@ def cpu_sample(st, a0, budget_s: float = 12.0):
                 oracle.sweep_f64(st, b, a)
         t1 = time.perf_counter() - t0
     gst = st.interior_points * sweeps / t1 / 1e9
-    return {"value": gst, "unit": "GStencil/s", "cores": oracle.max_threads(), "kind": "port",
+    cores = oracle.max_threads()
+    return {"value": gst, "unit": "GStencil/s", "cores": cores, "kind": "port",
+            "how": f"oracle port of the reference's serial loops on {cores} host threads",
             "sample": f"{sweeps} whole-grid sweep(s) of the {st.name} grid {tuple(st.sizes)} "
                       f"({st.interior_points} interior points each)", "seconds": t1}
+
+
+def cpu_sample_1thread(st, a0):
+    """The same port on one thread -- the reference's own CPU path is serial
+    (mpe_verify) -- for one whole-grid sweep."""
+    import oracle
+    a, b = a0.copy(), a0.copy()
+    oracle.set_threads(1)
+    try:
+        t0 = time.perf_counter()
+        oracle.sweep_f64(st, a, b)
+        t1 = time.perf_counter() - t0
+    finally:
+        oracle.set_threads(os.cpu_count() or 1)
+    return {"value": st.interior_points / t1 / 1e9, "unit": "GStencil/s", "cores": 1, "kind": "port",
+            "how": "oracle port of the reference's serial loops on 1 thread, as the reference runs them",
+            "sample": f"1 whole-grid sweep of the {st.name} grid {tuple(st.sizes)}", "seconds": t1}
 
 
 def run_reference(args, rank: int, world: int):
@@ -188,8 +239,7 @@ def run_reference(args, rank: int, world: int):
             "warmup": args.warmup, "ms_per_step": samp["seconds"] * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
             "impl": "reference",
-            "config": {"workload": f"{st.name} {st.interior_points ** (1 / st.rank):.0f}^{st.rank} T={st.iterations}",
-                       "l2": "inputs larger than L2"},
+            "config": {"workload": workload_label(st), "l2": "inputs larger than L2 (no flush)"},
             "cpu_baseline": samp,
             "e2e": {"value": v, "unit": "GStencil/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -285,25 +335,44 @@ def box_paths(uhs, args, stream):
 
 
 def timed_runs(uhs, st, a, b, params, steps, warmup, stream, dist=None):
+    """Time `steps` runs of the program, each on the workload's own input:
+    before every run (outside the timed interval) both grids are reset to the
+    input that a held at entry, so every step sweeps the same data rather than
+    the previous step's result.  Each run is bracketed by CUDA events on the
+    launching stream; returns the summed milliseconds and the kernels launched
+    inside the timed intervals."""
     import torch
+    a0 = a.clone()
+
+    def reset():
+        a.copy_(a0)
+        b.copy_(a0)
+
     for _ in range(warmup):
+        reset()
         uhs.run(st, a, b, params, stream=stream)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    n0 = uhs.launch_count()
-    e0.record(stream)
-    for _ in range(steps):
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    launches = 0
+    for e0, e1 in ev:
+        reset()
+        n0 = uhs.launch_count()
+        e0.record(stream)
         uhs.run(st, a, b, params, stream=stream)
-    e1.record(stream)
+        e1.record(stream)
+        launches += uhs.launch_count() - n0
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    ms = e0.elapsed_time(e1)
-    return ms, uhs.launch_count() - n0
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in ev)
+    a.copy_(a0)
+    b.copy_(a0)
+    torch.cuda.synchronize()
+    del a0
+    return ms, launches
 
 
 def bench_batch(args, rank: int, world: int, local: int):
@@ -569,7 +638,7 @@ def main():
             ms32, _ = timed_runs(uhs, st32, a32, b32, uhs.RunParams(flags=uhs._lib.UHS_FLAG_NO_SYNC),
                                  args.steps, args.warmup, stream, dist)
         fp32 = {"value": pts * args.steps / (ms32 * 1e-3) / 1e9, "unit": "GStencil/s",
-                "speedup_vs_f64": ms / ms32}
+                "speedup_vs_f64_auto": ms / ms32}
         if errs is not None:
             a32.copy_(torch.from_numpy(a0.astype(np.float32).reshape(st.sizes)))
             b32.copy_(a32)
@@ -591,6 +660,36 @@ def main():
         fp32["l2_rel_vs_f64_gpu"] = e["l2_rel"]
         fp32["max_rel_vs_f64_gpu"] = e["max_rel"]
         del a32, b32
+
+    # Plain FP64: the same program in native IEEE binary64 arithmetic (one
+    # DFMA per term and point, the arithmetic of the reference's GPU kernel),
+    # timed the same way; its sweep kernel's rate against the HBM roofline and
+    # against the FP64 pipe's DFMA rate measured here.
+    plain = None
+    if st.dtype == uhs.UHS_F64 and args.arith == 0 and not args.no_plain:
+        pparams = uhs.RunParams(kernel=args.kernel, arith=uhs._lib.UHS_ARITH_FMA, flags=uhs._lib.UHS_FLAG_NO_SYNC)
+        dev_a.copy_(torch.from_numpy(a0.reshape(st.sizes)))
+        dev_b.copy_(dev_a)
+        with torch.cuda.stream(stream):
+            msp, _ = timed_runs(uhs, st, dev_a, dev_b, pparams, max(2, args.steps // 2), args.warmup, stream, dist)
+        msp = reduce_max_ms(msp, dist, "cuda") / max(2, args.steps // 2)
+        pplan = uhs.plan(st, dev_a, pparams)
+        with torch.cuda.stream(stream):
+            pk_ms = sweep_launch_ms(uhs, st, dev_a, dev_b, pplan, stream, n=10)
+            dfma = uhs.probe_dfma_rate(stream)
+        gst_p = pts / (msp * 1e-3) / 1e9
+        plain = {"value": gst_p, "unit": "GStencil/s", "arith": ARITH_LABELS[1], "ms_per_step": msp,
+                 "kernel_ms": pk_ms, "hbm_frac": alg_bytes / (pk_ms * 1e-3) / 1e9 / peak,
+                 "dfma_per_s_measured": dfma,
+                 "dfma_frac": st.interior_points * len(st.terms) / (pk_ms * 1e-3) / dfma,
+                 "bound": "fp64 pipe (one DFMA per term and point)"}
+        if errs is not None:
+            dev_a.copy_(torch.from_numpy(a0.reshape(st.sizes)))
+            dev_b.copy_(dev_a)
+            uhs.run(st, dev_a, dev_b, uhs.RunParams(kernel=args.kernel, arith=uhs._lib.UHS_ARITH_FMA))
+            ep = oracle.error(st, ra, dev_a.cpu().numpy().reshape(-1))
+            plain["l2_rel_vs_oracle"] = ep["l2_rel"]
+            plain["max_rel_vs_oracle"] = ep["max_rel"]
 
     # End to end through the C ABI with host buffers: each step copies its
     # input grid from pinned host memory, runs the program (uhs_run) and reads
@@ -645,20 +744,35 @@ def main():
 
     if rank != 0:
         return
+    if cpu is not None:
+        cpu["single_thread"] = cpu_sample_1thread(st, a0)
+    # The metric's comparison: FP32 grids and the default FP64 path against
+    # plain FP64, each with its error against the FP64 oracle.
+    vs_plain = None
+    if plain is not None:
+        vs_plain = {"plain_f64_gstencil_s": plain["value"],
+                    "f64_auto": plain["ms_per_step"] / ms_step,
+                    "f64_auto_arith": arith_names_full(plan.arith),
+                    "f64_auto_l2_rel": errs["l2_rel"] if errs else None,
+                    "f64_auto_max_rel": errs["max_rel"] if errs else None}
+        if fp32 is not None:
+            fp32["speedup_vs_plain_f64"] = plain["ms_per_step"] / (ms32 / args.steps)
+            vs_plain["fp32"] = fp32["speedup_vs_plain_f64"]
+            vs_plain["fp32_l2_rel"] = fp32.get("l2_rel_vs_f64_oracle")
     arith_names = {1: "fma", 2: "exact", 3: "df32"}
     name = {0: "f64", 1: "f32"}.get(st.dtype, "f32x2")
-    star7 = st.rank == 3 and len(st.terms) == 7 and max(st.radius) == 1
     kname = "f32x2" if pair_resident else name
-    bpp = NCU_BYTES_PER_POINT.get(("star7", kname, arith_names.get(plan.arith, "")), None) if star7 else None
+    tkey = traffic_key(st, kname, arith_names.get(plan.arith, ""), plan.factored == 1)
+    bpp = NCU_BYTES_PER_POINT.get(tkey)
     traffic = bpp * st.interior_points if bpp else None
     if plan.kernel == uhs.UHS_KERNEL_MMA:
         name = "f32 (split-tf32 tensor cores)"
     line = {
         "metric": "GStencil/s", "value": value, "unit": "GStencil/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": name, "data": "synthetic (seeded SplitMix64)",
-        "config": {"workload": f"{st.name}: {'x'.join(str(u - l) for l, u in zip(st.lb, st.ub))} interior, "
-                               f"halo {st.lb[2]}, T={st.iterations}",
+        "vs_baseline": None, "dtype": name, "arith": ARITH_LABELS.get(plan.arith, str(plan.arith)),
+        "data": "synthetic (seeded SplitMix64)",
+        "config": {"workload": workload_label(st),
                    "parallelism": "replicas" if world > 1 else "1 GPU", "l2": "inputs larger than L2 (no flush)",
                    "kernel": plan.kernel, "arith": arith_names.get(plan.arith, plan.arith),
                    "tile": [plan.tile_x, plan.tile_y, plan.tile_z], "k_temporal": plan.k_temporal,
@@ -666,8 +780,9 @@ def main():
         "pct_hbm_roofline": achieved / peak,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic,
-                     "traffic_source": "ncu DRAM bytes of one launch of this kernel at 320^3, scaled by points"
-                     if traffic else None,
+                     "traffic_source": (f"ncu DRAM bytes per point of one launch of this kernel {tkey} on a "
+                                        "smaller grid, times the points" if traffic else
+                                        f"no ncu capture recorded for {tkey}"),
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "kernel": ("float-pair sweep on pair-resident copies of the FP64 grids" if pair_resident
                                 else "sweep on the grids in place"),
@@ -682,6 +797,8 @@ def main():
         "cpu_baseline": cpu,
         "error_vs_oracle": errs,
         "fp32": fp32,
+        "plain_f64": plain,
+        "speedup_vs_plain_f64": vs_plain,
     }
     if args.config == "cfg3" and not args.no_cpu:
         line["box_paths"] = box_paths(uhs, args, stream)

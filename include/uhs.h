@@ -57,13 +57,17 @@ enum {
 enum {
     UHS_ARITH_AUTO = 0,  /* the backend picks: for F64 grids on the streaming kernel,
                             UHS_ARITH_DF32 when a device scan of both grids shows
-                            max|x| * (sum|c|)^T < 2^119 (one extra read of each grid
-                            and one host round trip per call), else UHS_ARITH_FMA */
+                            max|x| * (sum|c|)^T < 2^120 and every nonzero |x| >= 2^-50
+                            (one extra read of each grid and one host round trip per
+                            call), else UHS_ARITH_FMA */
     UHS_ARITH_FMA = 1,   /* native arithmetic, products fused into the sum */
     UHS_ARITH_EXACT = 2, /* separately rounded products and sums in expression
                             order: bit-identical to the serial CPU loops */
-    UHS_ARITH_DF32 = 3   /* F64 grids computed in float-pair (~48-bit) arithmetic
-                            on the FP32 pipes; results within 1e-12 of FP64 */
+    UHS_ARITH_DF32 = 3   /* F64 grids computed in float-pair arithmetic on the FP32
+                            pipes: 48-bit significands in the float exponent range (a
+                            value between 2^-74 and 2^128 is held to 2^-48 of itself;
+                            below 2^-74 a pair keeps 24 bits, below 2^-126 it flushes
+                            to zero; 2^128 or more returns UHS_ERANGE) */
 };
 
 /* ---- MLIR memref descriptor (rank-3 layout) ---------------------------- */
@@ -174,10 +178,17 @@ int uhs_validate(const uhs_stencil_desc *desc, const uhs_memref *a, const uhs_me
  * floats once, the T sweeps read and write pairs, and the domain of both grids
  * is joined back to FP64 at the end.  The halo is read from the FP64 grids and
  * never written, so it stays bit-exact.  The copies (16 bytes per grid cell)
- * are stream-ordered allocations from the device's default memory pool, which
- * the library sets to keep freed memory for reuse (trim it with
- * cudaMemPoolTrimTo).  When that allocation fails, or with UHS_FLAG_IN_PLACE,
- * the sweeps run on the FP64 grids directly, splitting on every load. */
+ * are stream-ordered allocations from a memory pool the library owns on each
+ * device, which keeps freed memory for the next run (uhs_release_scratch
+ * returns it; the device's default pool is not touched).  When that
+ * allocation fails, or with UHS_FLAG_IN_PLACE, the sweeps run on the FP64
+ * grids directly, splitting on every load.
+ *
+ * Range: UHS_ARITH_AUTO keeps float pairs only when a scan of both grids
+ * finds no Inf/NaN, max|x| * (sum|c|)^T below 2^120 and every nonzero |x| at
+ * least 2^-50; otherwise the run computes in native FP64.  With either
+ * float-pair mode, a value that leaves the float range during the run (2^128
+ * or more) makes the call return UHS_ERANGE. */
 int uhs_run(const uhs_stencil_desc *desc, const uhs_memref *a, const uhs_memref *b,
             const uhs_params *params, void *stream);
 
@@ -217,8 +228,10 @@ int uhs_error_norms(const uhs_stencil_desc *desc, const uhs_memref *x, const uhs
  * the library's device memory: 4 * (UHS_NOALLOC_MAX_PARTIALS + 1) doubles,
  * 256 KiB, held on every GPU that loads the library until the process exits.
  * The call allocates and frees nothing.  Its first call on a device looks up the
- * array's device address (a one-time set-up), so make that first call before
- * any stream capture.  All calls on a device share the one array; each call
+ * array's device address (a set-up that loads the library's device code on
+ * that device if it is not loaded yet), so make that first call before any
+ * stream capture.  The address is kept for the device's context and looked
+ * up again after the context is destroyed and re-created (cudaDeviceReset).  All calls on a device share the one array; each call
  * rewrites every slot it reads, so nothing carries over between calls, but
  * calls whose kernels overlap on the GPU (other streams, other host threads)
  * race on it: serialise them.  Returns after the stream drained, out filled. */
@@ -306,6 +319,11 @@ int uhs_mlp_train(uhs_mlp *m, const float *x, const float *y, int32_t n, int32_t
 /* Number of kernels this library launched since load (diagnostics). */
 int64_t uhs_launch_count(void);
 
+/* Return the device memory the library's scratch pools keep for reuse (the
+ * float-pair copies of pair-resident runs) to the driver, on every device
+ * used so far.  Memory of runs still in flight is released when they end. */
+int uhs_release_scratch(void);
+
 /* Diagnostics: exercise the failure-reporting path.  Launches one CTA whose
  * mbarrier wait can never complete, bounded at `cycles` SM clocks (1 to 2^31;
  * 2^31 is the sweep kernels' bound, about one second at 2 GHz).  When the
@@ -314,6 +332,12 @@ int64_t uhs_launch_count(void);
  * faults and the device stays usable.  Returns UHS_ETIMEOUT with the message
  * the sweeps would give, after the stream drained. */
 int uhs_probe_wait_timeout(int64_t cycles, void *stream);
+
+/* Diagnostics: the FP64 pipe's rate on the current device, in DFMA per
+ * second -- the ceiling of a sweep in native FP64 arithmetic, which issues
+ * one DFMA per term and point.  Every SM runs independent DFMA chains for
+ * about 20 ms, timed with CUDA events on stream; returns after that. */
+int uhs_probe_dfma_rate(double *per_second, void *stream);
 
 /* Diagnostics: fail every library-owned device allocation larger than
  * `bytes` as an out-of-memory would (0 removes the cap), so callers can test

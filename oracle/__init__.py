@@ -133,6 +133,28 @@ def error(st, ref: np.ndarray, x: np.ndarray) -> dict:
     return {"l2_rel": out[0], "max_abs": out[1], "max_rel": out[2], "max_ref": out[3]}
 
 
+def cell_error(st, ref: np.ndarray, x: np.ndarray, floor: float = 0.0) -> float:
+    """Largest per-cell relative error over the domain,
+    max |x - ref| / max(|ref|, floor): unlike max_rel of error(), which
+    divides by the field's largest magnitude, it sees small cells that lost
+    precision.  Cells where both are equal count 0 (a zero reference cell
+    with floor 0 then counts only when x differs).  Chunked by planes."""
+    sz = st.sizes
+    r3 = ref.reshape(sz)
+    x3 = x.reshape(sz)
+    worst = 0.0
+    y0, y1, x0, x1 = st.lb[1], st.ub[1], st.lb[2], st.ub[2]
+    for z in range(st.lb[0], st.ub[0]):
+        r = r3[z, y0:y1, x0:x1]
+        d = np.abs(x3[z, y0:y1, x0:x1].astype(np.float64) - r)
+        den = np.maximum(np.abs(r), floor)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            q = np.where(d == 0.0, 0.0, d / den)
+        if q.size:
+            worst = max(worst, float(np.nanmax(np.where(np.isnan(q), np.inf, q))))
+    return worst
+
+
 def halo_diff(st, a: np.ndarray, b: np.ndarray) -> int:
     """Cells outside the domain whose bytes differ."""
     o = OracleStencil(st)

@@ -18,7 +18,9 @@ reference checkout, with:
 Flags: gcc/g++ -O2 -ffp-contract=off, the same as the oracle.
 
 Usage: python oracle/build_ref.py [REFERENCE_ROOT]
-Nothing is built when the reference checkout is absent.
+The checkout is found through reference_root(): the UHS_REFERENCE_ROOT
+environment variable, else the checkout's location on the build machine.
+Nothing is built when it is absent.
 """
 from __future__ import annotations
 
@@ -30,6 +32,15 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 SHIM = os.path.join(HERE, "shim")
+# where the reference checkout lies on the machine that builds the checker;
+# UHS_REFERENCE_ROOT overrides it
+_DEFAULT_ROOT = "/root/reference"
+
+
+def reference_root() -> str | None:
+    """The reference checkout, or None where it is absent (GPU machines)."""
+    root = os.environ.get("UHS_REFERENCE_ROOT") or _DEFAULT_ROOT
+    return root if os.path.isdir(os.path.join(root, "UH-SW")) else None
 
 # case -> (UH-SW driver, UH-GPU driver), paths relative to the reference root
 CASES = {
@@ -83,8 +94,9 @@ def _build_one(ref_root: str, tag: str, src_rel: str) -> str:
     return so
 
 
-def build(ref_root: str = "/root/reference") -> list[str]:
-    if not os.path.isdir(os.path.join(ref_root, "UH-SW")):
+def build(ref_root: str | None = None) -> list[str]:
+    ref_root = ref_root or reference_root()
+    if not ref_root or not os.path.isdir(os.path.join(ref_root, "UH-SW")):
         return []
     os.makedirs(OUT, exist_ok=True)
     jobs = []
@@ -96,5 +108,5 @@ def build(ref_root: str = "/root/reference") -> list[str]:
 
 
 if __name__ == "__main__":
-    built = build(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    built = build(sys.argv[1] if len(sys.argv) > 1 else None)
     print(f"built {len(built)} reference drivers into {OUT}")

@@ -98,4 +98,8 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    from oracle.build_ref import reference_root
+    root = sys.argv[1] if len(sys.argv) > 1 else reference_root()
+    if not root:
+        raise SystemExit("reference checkout not found (pass its path or set UHS_REFERENCE_ROOT)")
+    main(root)

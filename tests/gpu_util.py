@@ -39,3 +39,10 @@ def assert_f64_close(st, ref, got, tol=1e-12):
 
 def assert_halo_exact(st, ref, got):
     assert oracle.halo_diff(st, ref, got) == 0
+
+
+def assert_cells_close(st, ref, got, tol=1e-12, floor=0.0):
+    """Per-cell relative error (oracle.cell_error) within tol."""
+    e = oracle.cell_error(st, ref, got, floor)
+    assert e <= tol, e
+    return e

@@ -7,6 +7,7 @@ import subprocess
 import pytest
 
 from golden_util import load, reference_stencil
+from oracle.build_ref import reference_root
 from uxxxxxxxxh_gb300 import ciface
 
 CASES = sorted(load("reference_stencils.json"))
@@ -31,7 +32,7 @@ def test_single_sweep_program_exports_the_compute_function(tmp_path):
     assert f"_mlir_ciface_{st.name}_iteration" not in syms
 
 
-REF_DRIVER = "/root/reference/UH-GPU/3d1r_star/3d7pt_main.cpp"
+REF_DRIVER = os.path.join(reference_root() or "", "UH-GPU/3d1r_star/3d7pt_main.cpp")
 
 
 @pytest.mark.skipif(not os.path.exists(REF_DRIVER), reason="reference checkout not present")

@@ -16,7 +16,9 @@ import uxxxxxxxxh_gb300 as uhs
 from uxxxxxxxxh_gb300 import _lib
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference"
+from oracle.build_ref import reference_root
+
+REF = reference_root() or ""
 
 HEAT3D = """# seven-point heat step
 stencil heat3d(double t[18][20][22]) {

@@ -4,10 +4,11 @@ sin(x)cos(y)sin(z) + 1e-3 noise, run in FP32 grids, float-pair grids
 arithmetic; every 20 steps each is scored on the GPU (uhs_error_norms)
 against the FP64 oracle's state.
 
-Default size is 96^3, T = 200 (the suite's bars: FP64 paths and float pairs
-within 1e-12 of the oracle, FP32 within a relative L2 of 1e-6).  The full
-configuration (512^3, T = 200) runs with UHS_PRECISION_N=512; the table is
-written to UHS_PRECISION_OUT when that is set.
+It runs at 96^3 and at the configuration's full size, 512^3, both with
+T = 200 (the bars, at every 20th step: FP64 paths and float pairs within
+1e-12 of the oracle, FP32 within a relative L2 of 1e-6).  With
+UHS_PRECISION_N set only that size runs, and the table is written to
+UHS_PRECISION_OUT when that is set.
 """
 import json
 import os
@@ -24,9 +25,12 @@ from uxxxxxxxxh_gb300.workloads import cfg4
 pytestmark = pytest.mark.gpu
 
 
-def test_precision_study(cuda):
+SIZES = [int(os.environ["UHS_PRECISION_N"])] if os.environ.get("UHS_PRECISION_N") else [96, 512]
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_precision_study(cuda, n):
     import torch
-    n = int(os.environ.get("UHS_PRECISION_N", "96"))
     T, every = 200, 20
     oracle.set_threads(os.cpu_count() or 1)
     st, a0 = cfg4(n=n, T=T)
@@ -69,3 +73,7 @@ def test_precision_study(cuda):
         for k in ("f32x2", "f64_df32", "f64_native"):
             assert row[k]["max_rel"] <= 1e-12, (row["step"], k, row[k])
         assert row["f32"]["l2_rel"] <= 1e-6, (row["step"], row["f32"])
+    # the FP64 grids' halos are never written: bit-identical to the oracle's
+    for k in ("f64_df32", "f64_native"):
+        for g, r in zip(grids[k], (ra, rb)):
+            assert oracle.halo_diff(st, r, g.cpu().numpy().reshape(-1)) == 0, k

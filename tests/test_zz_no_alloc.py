@@ -67,3 +67,29 @@ def test_noalloc_takes_a_domain_of_any_size(cuda):
         assert rc == _lib.UHS_OK, _lib.last_error()
         want = uhs.error_norms(st, x, r)
         assert got == want and got["l2_rel"] > 0.0
+
+
+def test_noalloc_leaves_device_memory_untouched(cuda):
+    """The entry point's promise: no device allocation.  After one warm-up
+    call (which loads the library's device code on first use), the device's
+    free memory is the same before and after further calls on a fresh
+    stream."""
+    import torch
+    st, ref = random_case(3, 1, "star", (40, 44, 72), 2, 77)
+    r = to_dev(ref, st)
+    x = r + 1e-9 * torch.randn_like(r)
+    stream = torch.cuda.Stream()
+    d = st.to_desc()
+    mx, mr = uhs.memref_of(x), uhs.memref_of(r)
+    out = (ctypes.c_double * 4)()
+    lib = _lib.lib()
+    assert lib.uhs_error_norms_noalloc(d.ref(), ctypes.byref(mx), ctypes.byref(mr), out, None) == _lib.UHS_OK
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        rc = lib.uhs_error_norms_noalloc(d.ref(), ctypes.byref(mx), ctypes.byref(mr), out, stream.cuda_stream)
+        assert rc == _lib.UHS_OK, _lib.last_error()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert out[0] > 0.0

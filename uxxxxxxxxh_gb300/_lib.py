@@ -68,7 +68,9 @@ SIGNATURES = {
     "uhs_sweep": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Memref), POINTER(Params), c_void_p]),
     "uhs_plan": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Params), POINTER(Params)]),
     "uhs_launch_count": (c_int64, []),
+    "uhs_release_scratch": (c_int, []),
     "uhs_probe_wait_timeout": (c_int, [c_int64, c_void_p]),
+    "uhs_probe_dfma_rate": (c_int, [POINTER(c_double), c_void_p]),
     "uhs_set_alloc_cap": (c_int, [c_int64]),
     "uhs_tune_save": (c_int, [c_char_p]),
     "uhs_tune_load": (c_int, [c_char_p]),

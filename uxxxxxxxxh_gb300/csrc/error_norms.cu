@@ -17,6 +17,8 @@
 // The sums stay in FP64 (3 FP64 operations per point: the difference and two
 // squares), which bounds the kernel by GB300's FP64 pipe rather than HBM;
 // the maxima run on the integer pipes.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "uhs_kernels.h"
@@ -224,24 +226,67 @@ cudaError_t launch_error_norms(const ErrNormsCall &c) {
 
 }  // namespace uhs
 
-// One-time set-up per device, with that device current: the device address
-// of g_noalloc_scratch.  Returns nullptr (and sets the error) on failure.
+// Identity of the calling thread's current CUDA context (the device's
+// primary context once the runtime has set the device), through the driver
+// entry points; 0 when they are unavailable.  cudaDeviceReset destroys the
+// primary context and the next runtime call creates another with a new id,
+// in which the array has a new device address.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+
+static unsigned long long current_context_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(p);
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(p);
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
+
+// Set-up, once per device and context, with that device current: the device
+// address of g_noalloc_scratch (a lookup: it allocates nothing).  The
+// address is kept with the id of the context it belongs to and looked up
+// again when the device's context has changed (after cudaDeviceReset), or on
+// every call when the context id cannot be read.  Returns nullptr (and sets
+// the error) on failure.
 static double *noalloc_scratch(int dev) {
     static std::mutex mu;
     static double *addr[64] = {};
+    static unsigned long long ctx_of[64] = {};
     if (dev < 0 || dev >= 64) {
         uhs::set_error(UHS_EUNSUPPORTED, "device ordinal %d is beyond the 64 this library tracks", dev);
         return nullptr;
     }
+    // make the device's primary context current on this thread (cudaSetDevice
+    // initialises it), so the id read below is the one the launches will use
+    cudaError_t e = cudaSetDevice(dev);
+    if (e != cudaSuccess) {
+        uhs::set_error(UHS_ECUDA, "cudaSetDevice(%d): %s", dev, cudaGetErrorString(e));
+        return nullptr;
+    }
+    const unsigned long long ctx = current_context_id();
     std::lock_guard<std::mutex> lk(mu);
-    if (!addr[dev]) {
+    if (!addr[dev] || ctx == 0 || ctx != ctx_of[dev]) {
         void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) {
             uhs::set_error(UHS_ECUDA, "cudaGetSymbolAddress of the reduction scratch: %s", cudaGetErrorString(e));
             return nullptr;
         }
         addr[dev] = static_cast<double *>(p);
+        ctx_of[dev] = ctx;
     }
     return addr[dev];
 }

@@ -55,10 +55,13 @@ __global__ void __launch_bounds__(kConvThreads) k_to_pairs(const PairConv a) {
 }
 
 // pairs -> FP64 over the domain [lb, ub): each value the double nearest
-// hi + lo.  One warp per row at a time.
+// hi + lo.  One warp per row at a time.  A pair whose hi is Inf or NaN grew
+// out of the float range during the sweeps: the range flag is set, as a
+// split of an out-of-range value does.
 __global__ void __launch_bounds__(kConvThreads) k_from_pairs(const PairConv a) {
     const int64_t ny = a.ub1 - a.lb1, rows = (a.ub0 - a.lb0) * ny;
     const int wpb = kConvThreads / 32, lane = threadIdx.x & 31;
+    unsigned rerr = 0;
     for (int64_t row = static_cast<int64_t>(blockIdx.x) * wpb + (threadIdx.x >> 5); row < rows;
          row += static_cast<int64_t>(gridDim.x) * wpb) {
         const int64_t z = a.lb0 + row / ny, y = a.lb1 + row % ny;
@@ -67,15 +70,18 @@ __global__ void __launch_bounds__(kConvThreads) k_from_pairs(const PairConv a) {
 #pragma unroll 4
         for (int64_t x = a.lb2 + lane; x < a.ub2; x += 32) {
             const float2 v = s[x];
+            rerr |= (__float_as_uint(v.x) & 0x7f800000u) == 0x7f800000u;
             d[x] = join_f64(v.x, v.y);
         }
     }
+    if (rerr) atomicOr(a.err, kDevErrRange);
 }
 
 // CTAs of 8 warps, one row per warp at a time: at most 8 resident CTAs on
-// each of 152 SMs.
+// each SM.
 unsigned conv_blocks(int64_t rows) {
-    const int64_t need = (rows + kConvThreads / 32 - 1) / (kConvThreads / 32), cap = int64_t(152) * 8;
+    const int64_t need = (rows + kConvThreads / 32 - 1) / (kConvThreads / 32),
+                  cap = static_cast<int64_t>(device_sm_count()) * 8;
     return static_cast<unsigned>(need < 1 ? 1 : need < cap ? need : cap);
 }
 
@@ -92,9 +98,9 @@ cudaError_t launch_to_pairs(const GridView &src, const GridView &dst, const int6
 }
 
 cudaError_t launch_from_pairs(const GridView &src, const GridView &dst, const int64_t lb[3], const int64_t ub[3],
-                              cudaStream_t st) {
+                              unsigned *err, cudaStream_t st) {
     PairConv a{src.data, dst.data, src.s[0], src.s[1], dst.s[0], dst.s[1], src.n[0], src.n[1], src.n[2],
-               lb[0], lb[1], lb[2], ub[0], ub[1], ub[2], 0, nullptr};
+               lb[0], lb[1], lb[2], ub[0], ub[1], ub[2], 0, err};
     const int64_t rows = (ub[0] - lb[0]) * (ub[1] - lb[1]);
     if (rows <= 0 || ub[2] <= lb[2]) return cudaSuccess;
     k_from_pairs<<<conv_blocks(rows), kConvThreads, 0, st>>>(a);

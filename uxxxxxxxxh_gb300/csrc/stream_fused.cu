@@ -68,7 +68,7 @@ struct FArith<C, kArNative> {  // float grids: centre correction as in Arith (st
         if constexpr (F32) s = fmaf(a.cl_sum, v, s);
     }
     __device__ static T level(const Acc &s) { return s; }
-    __device__ static void store(T *p, const Acc &s) { *p = s; }
+    __device__ static void store(T *p, const Acc &s, unsigned &) { *p = s; }
 };
 template <class C>
 struct FArith<C, kArDf32> {
@@ -79,7 +79,11 @@ struct FArith<C, kArDf32> {
     __device__ static void add(Acc &s, const FusedArgs &a, int k, float2 v) { df_fma(s, a.chl[k].x, a.chl[k].y, v); }
     __device__ static void centre(Acc &, const FusedArgs &, float2) {}
     __device__ static float2 level(const Acc &s) { return renorm(s); }
-    __device__ static void store(double *p, const Acc &s) { *p = join_f64(s.h, s.l); }
+    // a sum that outgrew the float range sets the range flag (as in Arith)
+    __device__ static void store(double *p, const Acc &s, unsigned &range_err) {
+        range_err |= (__float_as_uint(s.h) & 0x7f800000u) == 0x7f800000u;
+        *p = join_f64(s.h, s.l);
+    }
 };
 
 template <class C>
@@ -168,7 +172,7 @@ __global__ void __launch_bounds__(256) k_fused(const __grid_constant__ FusedArgs
                     else v = lv(j - 1, sp_, e);
                     rings[((j - 1) * 3 + sp_ % 3) * PLANE + e] = v;
                 } else if (in_dom) {
-                    A::store(static_cast<TS *>(a.out) + p * a.out_s0 + gy * a.out_s1 + gx, acc);
+                    A::store(static_cast<TS *>(a.out) + p * a.out_s0 + gy * a.out_s1 + gx, acc, range_err);
                 }
             }
             __syncthreads();

@@ -224,7 +224,7 @@ struct Arith<C, kArNative> {
     __device__ static __forceinline__ void centre(Acc &acc, const Args &a, int pass, TS v) {
         if constexpr (F32) acc = fmaf(a.cl_sum[pass], v, acc);
     }
-    __device__ static __forceinline__ void store(TS *p, const Acc &acc) { *p = acc; }
+    __device__ static __forceinline__ void store(TS *p, const Acc &acc, unsigned &) { *p = acc; }
     __device__ static __forceinline__ TS level(const Acc &acc) { return acc; }
 };
 
@@ -241,9 +241,16 @@ struct Arith<C, kArDf32> {
         const float2 c = coef_f2<C>(a, k);
         df_fma(acc, c.x, c.y, v);
     }
-    __device__ static __forceinline__ void store(typename C::TS *p, const Acc &acc) {
-        if constexpr (C::ST == kStF64) *p = join_f64(acc.h, acc.l);
-        else *p = renorm(acc);
+    // FP64 grids: a sum that outgrew the float range (hi Inf or NaN) would
+    // join to a finite double near 2^128; it sets the range flag instead of
+    // passing unnoticed.
+    __device__ static __forceinline__ void store(typename C::TS *p, const Acc &acc, unsigned &range_err) {
+        if constexpr (C::ST == kStF64) {
+            range_err |= (__float_as_uint(acc.h) & 0x7f800000u) == 0x7f800000u;
+            *p = join_f64(acc.h, acc.l);
+        } else {
+            *p = renorm(acc);
+        }
     }
     __device__ static __forceinline__ float2 level(const Acc &acc) { return renorm(acc); }
     template <class Args>
@@ -573,7 +580,7 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
             }
 #pragma unroll
             for (int v = 0; v < VY; ++v)
-                if (v < vmax) A::store(optr + v * a.out_s1, acc[v]);
+                if (v < vmax) A::store(optr + v * a.out_s1, acc[v], range_err);
             optr += a.out_s0;
         }
         // advance the rings

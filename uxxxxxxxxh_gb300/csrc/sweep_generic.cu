@@ -181,9 +181,10 @@ cudaError_t launch_t(const SweepSpec &sp, const LaunchCfg &cfg, const GridView &
     const int64_t tiles = ((nx + TX - 1) / TX) * ((ny + TY - 1) / TY);
     int zchunk = cfg.tile_z;
     if (zchunk <= 0) {
-        // Enough CTAs to fill 152 SMs several times over, chunks long enough
+        // Enough CTAs to fill the SMs several times over, chunks long enough
         // that the 2*rz warm-up planes stay a small fraction.
-        const int64_t want_chunks = std::max<int64_t>(1, (152 * 16 + tiles - 1) / tiles);
+        const int64_t want = static_cast<int64_t>(device_sm_count()) * 16;
+        const int64_t want_chunks = std::max<int64_t>(1, (want + tiles - 1) / tiles);
         zchunk = (int)std::max<int64_t>(std::max(8, 4 * sp.rz), (nz + want_chunks - 1) / want_chunks);
     }
     a.zchunk = (int)std::min<int64_t>(zchunk, nz);

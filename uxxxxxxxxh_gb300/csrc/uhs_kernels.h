@@ -41,6 +41,11 @@ struct LaunchCfg {
 // Device-side error word written by kernels that detect a problem (range
 // overflow in float-pair arithmetic, a bounded wait that ran out).
 enum : unsigned { kDevErrRange = 1u, kDevErrTimeout = 2u };
+// A status word is kStatusWords unsigned words in device memory:
+//   0 kernel status flags; 1 range-scan largest exponent / halo-check count;
+//   2-7 where the first bounded wait gave up (set, block x, block z, plane,
+//   ring slot, phase); 8 range-scan smallest exponent of a nonzero value.
+constexpr int kStatusWords = 16;
 unsigned *stream_error_word(int device, cudaStream_t stream);
 
 // Generic smem plane-ring sweep: any term list, expression order.
@@ -53,9 +58,12 @@ cudaError_t launch_generic(const SweepSpec &sp, const LaunchCfg &cfg, const Grid
 // elements); at most kErrBlocks CTAs take the units round-robin, each writing
 // 4 doubles of partials into scratch; the result (4 doubles) follows the
 // partials.  Scratch holds 4 * (nblocks + 1) doubles.  The split depends only
-// on the domain's shape, so results are the same on every device.
+// on the domain's shape, never on the device, so the FP64 sums are added in
+// the same order and the results are the same on every GPU: kErrBlocks is a
+// fixed count (608, four resident 256-thread CTAs on each of a GB300's 152
+// SMs), not the queried SM count.
 constexpr int kErrRowsPerUnit = 16;
-constexpr int64_t kErrBlocks = 4 * 152;  // 4 resident 256-thread CTAs per SM
+constexpr int64_t kErrBlocks = 608;
 inline void err_split(int64_t rows, int64_t width, int64_t *units, int *xchunks, int *nblocks) {
     const int64_t ru = (rows + kErrRowsPerUnit - 1) / kErrRowsPerUnit, want = 8 * kErrBlocks;
     int64_t xc = 1;
@@ -86,12 +94,17 @@ cudaError_t launch_error_norms(const ErrNormsCall &c);
 // domain [lb, ub)), and the domain of a float-pair grid joined back.
 cudaError_t launch_to_pairs(const GridView &src, const GridView &dst, const int64_t lb[3], const int64_t ub[3],
                             bool halo_only, unsigned *err, cudaStream_t st);
+// The join sets kDevErrRange in *err when a pair holds Inf or NaN (a value
+// that outgrew the float range during the sweeps).
 cudaError_t launch_from_pairs(const GridView &src, const GridView &dst, const int64_t lb[3], const int64_t ub[3],
-                              cudaStream_t st);
+                              unsigned *err, cudaStream_t st);
 
-// Max of the biased exponent fields of n_words doubles into *out (atomicMax;
-// *out must start at 0).
-cudaError_t launch_max_exponent(const void *data, int64_t n_words, unsigned *out, int sms, cudaStream_t st);
+// Exponent range of n_words doubles: the largest biased exponent field into
+// *max_out (atomicMax; must start at 0) and the smallest biased exponent field
+// of a nonzero value (zeros of either sign are skipped; a subnormal counts as
+// exponent 0) into *min_out (atomicMin; must start at 0xffffffff).
+cudaError_t launch_exponent_range(const void *data, int64_t n_words, unsigned *max_out, unsigned *min_out, int sms,
+                                  cudaStream_t st);
 
 // FP32 3D box stencils of radius 2 and 3 on the tensor cores (box_mma.cu).
 // Coefficients in box slot order ((dz+R)*D + (dy+R))*D + (dx+R), D = 2R+1.
@@ -111,6 +124,8 @@ cudaError_t launch_box_mma(const MmaCall &c);
 
 // Failure-reporting probe (diag.cu): a bounded wait that cannot complete.
 cudaError_t launch_wait_probe(unsigned *err, long long cycles, cudaStream_t st);
+// FP64 pipe rate (diag.cu): DFMA per second over all SMs, timed on st.
+cudaError_t probe_dfma_rate(double *per_second, cudaStream_t st);
 
 // Library-owned device allocations go through dev_alloc, which honours the
 // diagnostic cap set by uhs_set_alloc_cap (a request above the cap fails as
@@ -119,5 +134,9 @@ cudaError_t dev_alloc(void **p, size_t bytes);
 
 // Launch counter shared by every launcher.
 void count_launch(int n = 1);
+
+// Streaming multiprocessors of the current device (queried once per device;
+// 1 if the query fails, which only shrinks the grids the launchers size).
+int device_sm_count();
 
 }  // namespace uhs

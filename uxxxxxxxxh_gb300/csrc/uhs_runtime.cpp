@@ -68,13 +68,9 @@ static int cuda_error(cudaError_t e, const char *what) {
     return set_error(UHS_ECUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
 }
 
-// Per-device error word (see uhs_kernels.h).  Allocated on first use.
-// Status words (8 x unsigned) in device memory, one per (device, stream),
-// allocated at first use and kept for the process:
-//   word 0: kernel status flags; word 1: range-scan / halo-check result;
-//   words 2-7: where the first bounded wait gave up (set, block x, block z,
-//   plane, ring slot, phase).
-// Calls on different streams (or host threads with their own streams) never
+// Status words (kStatusWords x unsigned, layout in uhs_kernels.h) in device
+// memory, one per (device, stream), allocated at first use and kept for the
+// process.  Calls on different streams (or host threads with their own streams) never
 // share a word, so one call's errors and scan results cannot leak into
 // another's.
 unsigned *stream_error_word(int device, cudaStream_t stream) {
@@ -85,8 +81,8 @@ unsigned *stream_error_word(int device, cudaStream_t stream) {
     auto it = words.find(key);
     if (it != words.end()) return it->second;
     void *p = nullptr;
-    if (dev_alloc(&p, 8 * sizeof(unsigned)) != cudaSuccess) return nullptr;
-    if (cudaMemset(p, 0, 8 * sizeof(unsigned)) != cudaSuccess) {
+    if (dev_alloc(&p, kStatusWords * sizeof(unsigned)) != cudaSuccess) return nullptr;
+    if (cudaMemset(p, 0, kStatusWords * sizeof(unsigned)) != cudaSuccess) {
         cudaFree(p);
         return nullptr;
     }
@@ -217,15 +213,21 @@ struct Plan {
     bool a_tmem = false;       // tensor-core path: A operand staged in tensor memory
 };
 
-static int device_sms() {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+int device_sm_count() {
+    static std::atomic<int> cached[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 1;
+    if (dev < 64 && cached[dev].load(std::memory_order_relaxed) > 0) return cached[dev].load(std::memory_order_relaxed);
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+        cudaGetLastError();
+        return 1;
     }
+    if (dev < 64) cached[dev].store(sms, std::memory_order_relaxed);
     return sms;
 }
+
+static int device_sms() { return device_sm_count(); }
 
 static int coef_slot_rt(int shape, int R, int dz, int dy, int dx) {
     const int D = 2 * R + 1;
@@ -592,29 +594,44 @@ static GridView kernel_view(const SweepSpec &sp, const GridView &v) {
     return k;
 }
 
-// UHS_ARITH_AUTO on FP64 grids: float pairs represent magnitudes below 2^128.
-// Scan both grids for their largest exponent and bound the growth over T
-// sweeps by (sum |c|)^T; fall back to native FP64 when the bound comes within
-// 2^8 of the limit, or when a grid holds Inf/NaN.
+// UHS_ARITH_AUTO on FP64 grids: a float pair holds a value to 2^-48 of
+// itself between 2^-74 and 2^128 (df32.cuh).  Scan both grids (their whole
+// spans, halo included) for their exponent range and keep float pairs only
+// when
+//   * no cell holds Inf or NaN;
+//   * the largest magnitude grown by (sum |c|)^T over the run stays below
+//     2^120 (8 binades under the float range);
+//   * every nonzero magnitude is at least 2^kPairMinExp, 24 binades above
+//     2^-74, so every input value is split exactly to 48 bits and values the
+//     run brings down by up to 2^24 still are.
+// Otherwise the run computes in native FP64.  Below 2^-74 a pair keeps 24
+// significant bits and below 2^-126 it flushes to zero, so without the
+// second bound a field spanning 1 ... 1e-30 would lose precision in its small
+// cells while a max-normalised error would not show it.
+constexpr int kPairMinExp = -50;
 static bool range_ok(const SweepSpec &sp, const GridView &a, const GridView &b, int T, cudaStream_t st) {
     int dev = 0;
     cudaGetDevice(&dev);
     unsigned *w = stream_error_word(dev, st);
     if (!w) return false;
-    unsigned *scan = w + 1;
-    if (cudaMemsetAsync(scan, 0, sizeof(unsigned), st) != cudaSuccess) return false;
+    unsigned *emax = w + 1, *emin = w + 8;
+    if (cudaMemsetAsync(emax, 0, sizeof(unsigned), st) != cudaSuccess) return false;
+    if (cudaMemsetAsync(emin, 0xff, sizeof(unsigned), st) != cudaSuccess) return false;
     for (const GridView *g : {&a, &b}) {
         const int64_t span = (g->n[0] - 1) * g->s[0] + (g->n[1] - 1) * g->s[1] + g->n[2];
-        if (launch_max_exponent(g->data, span, scan, device_sms(), st) != cudaSuccess) return false;
+        if (launch_exponent_range(g->data, span, emax, emin, device_sms(), st) != cudaSuccess) return false;
     }
-    unsigned e = 0;
-    if (cudaMemcpyAsync(&e, scan, sizeof e, cudaMemcpyDeviceToHost, st) != cudaSuccess) return false;
+    unsigned e[2] = {0u, 0u};
+    if (cudaMemcpyAsync(&e[0], emax, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess) return false;
+    if (cudaMemcpyAsync(&e[1], emin, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess) return false;
     if (cudaStreamSynchronize(st) != cudaSuccess) return false;
-    if (e >= 0x7ffu) return false;  // Inf or NaN somewhere
+    if (e[0] >= 0x7ffu) return false;  // Inf or NaN somewhere
+    // all cells zero: e[1] stays 0xffffffff, which passes
+    if (e[1] != 0xffffffffu && static_cast<int>(e[1]) - 1023 < kPairMinExp) return false;
     double csum = 0.0;
     for (int k = 0; k < sp.nterms; ++k) csum += std::fabs(sp.coef[k]);
     const double growth = csum > 1.0 ? std::max(T, 1) * std::log2(csum) : 0.0;
-    return static_cast<double>(static_cast<int>(e) - 1023) + 1.0 + growth < 120.0;
+    return static_cast<double>(static_cast<int>(e[0]) - 1023) + 1.0 + growth < 120.0;
 }
 
 static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in, const GridView &out,
@@ -989,7 +1006,8 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
     std::vector<std::vector<int4>> items(kNumPacks);
     {
         void *q = nullptr;
-        if (dev_alloc(&q, 8 * sizeof(unsigned)) != cudaSuccess || cudaMemset(q, 0, 8 * sizeof(unsigned)) != cudaSuccess)
+        if (dev_alloc(&q, kStatusWords * sizeof(unsigned)) != cudaSuccess ||
+            cudaMemset(q, 0, kStatusWords * sizeof(unsigned)) != cudaSuccess)
             return set_error(UHS_ENOMEM, "batch status word allocation failed");
         B->d_status = static_cast<unsigned *>(q);
     }
@@ -1268,8 +1286,8 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
                     }
                     if (rc) break;
                     if (g.pairs) {  // both domains back (T >= 8 sweeps wrote both grids)
-                        e = launch_from_pairs(g.pa, g.va, g.sp.lb, g.sp.ub, bs_[k]);
-                        if (e == cudaSuccess) e = launch_from_pairs(g.pb, g.vb, g.sp.lb, g.sp.ub, bs_[k]);
+                        e = launch_from_pairs(g.pa, g.va, g.sp.lb, g.sp.ub, err, bs_[k]);
+                        if (e == cudaSuccess) e = launch_from_pairs(g.pb, g.vb, g.sp.lb, g.sp.ub, err, bs_[k]);
                         launches += 2;
                         if (e != cudaSuccess) break;
                     }
@@ -1383,28 +1401,44 @@ static const uhs_params *effective_params(const uhs_stencil_desc *d, const uhs_p
     buf->flags = p ? p->flags : 0;
     return buf;
 }
-// Stream-ordered scratch from the device's default memory pool, which is set
-// once per device to keep freed memory for reuse (later runs then allocate
-// without a device-wide synchronisation).  Honours the diagnostic cap.
+// Stream-ordered scratch from a memory pool the library creates on each
+// device, set to keep freed memory for reuse (later runs then allocate
+// without a device-wide synchronisation).  The device's default pool, which
+// the host application may use, is left as it is.  uhs_release_scratch trims
+// these pools.  Honours the diagnostic cap.
+static std::mutex g_pool_mu;
+static cudaMemPool_t g_pools[64] = {};
+
+static cudaMemPool_t scratch_pool(int dev) {
+    if (dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (!g_pools[dev]) {
+        cudaMemPoolProps props;
+        std::memset(&props, 0, sizeof props);
+        props.allocType = cudaMemAllocationTypePinned;
+        props.handleTypes = cudaMemHandleTypeNone;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        g_pools[dev] = pool;
+    }
+    return g_pools[dev];
+}
+
 static cudaError_t dev_alloc_async(void **p, size_t bytes, cudaStream_t st) {
     const int64_t cap = g_alloc_cap.load(std::memory_order_relaxed);
     if (cap > 0 && static_cast<int64_t>(bytes) > cap) return cudaErrorMemoryAllocation;
     int dev = 0;
     cudaGetDevice(&dev);
-    static std::mutex mu;
-    static bool kept[64] = {};
-    if (dev >= 0 && dev < 64) {
-        std::lock_guard<std::mutex> lk(mu);
-        if (!kept[dev]) {
-            cudaMemPool_t pool;
-            if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
-                uint64_t keep = UINT64_MAX;
-                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
-            }
-            kept[dev] = true;
-        }
-    }
-    const cudaError_t e = cudaMallocAsync(p, bytes, st);
+    cudaMemPool_t pool = scratch_pool(dev);
+    if (!pool) return cudaErrorMemoryAllocation;
+    const cudaError_t e = cudaMallocFromPoolAsync(p, bytes, pool, st);
     if (e != cudaSuccess) cudaGetLastError();  // not sticky: the caller falls back
     return e;
 }
@@ -1415,6 +1449,13 @@ static cudaError_t dev_alloc_async(void **p, size_t bytes, cudaStream_t st) {
 static int run_pair_resident(const SweepSpec &sp, const uhs_params *p, const GridView &va, const GridView &vb,
                              int T, cudaStream_t st, bool *ran) {
     *ran = false;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    unsigned *err = stream_error_word(dev, st);
+    if (!err) {
+        *ran = true;  // report the failure instead of sweeping in place
+        return set_error(UHS_ENOMEM, "device error word allocation failed");
+    }
     const int64_t n0 = va.n[0], n1 = va.n[1], n2 = va.n[2];
     const size_t bytes = static_cast<size_t>(n0 * n1 * n2) * sizeof(double);
     void *buf = nullptr;
@@ -1438,9 +1479,6 @@ static int run_pair_resident(const SweepSpec &sp, const uhs_params *p, const Gri
         return UHS_OK;
     }
     *ran = true;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    unsigned *err = stream_error_word(dev, st);
     int rc = UHS_OK;
     cudaError_t e = launch_to_pairs(va, pa, sp.lb, sp.ub, false, err, st);
     if (e == cudaSuccess) e = launch_to_pairs(vb, pb, sp.lb, sp.ub, true, err, st);
@@ -1450,8 +1488,8 @@ static int run_pair_resident(const SweepSpec &sp, const uhs_params *p, const Gri
         rc = launch_sweep(sp2, pl2, pb, pa, st);
     }
     if (rc == UHS_OK) {
-        e = launch_from_pairs(pa, va, sp.lb, sp.ub, st);
-        if (e == cudaSuccess) e = launch_from_pairs(pb, vb, sp.lb, sp.ub, st);
+        e = launch_from_pairs(pa, va, sp.lb, sp.ub, err, st);
+        if (e == cudaSuccess) e = launch_from_pairs(pb, vb, sp.lb, sp.ub, err, st);
         if (e != cudaSuccess) rc = cuda_error(e, "float-pair conversion");
     }
     cudaFreeAsync(buf, st);
@@ -1474,6 +1512,16 @@ void uhs_params_default(uhs_params *p) {
 
 int64_t uhs_launch_count(void) { return g_launches.load(); }
 
+int uhs_release_scratch(void) {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    for (int dev = 0; dev < 64; ++dev) {
+        if (!g_pools[dev]) continue;
+        const cudaError_t e = cudaMemPoolTrimTo(g_pools[dev], 0);
+        if (e != cudaSuccess) return cuda_error(e, "scratch pool trim");
+    }
+    return UHS_OK;
+}
+
 int uhs_probe_wait_timeout(int64_t cycles, void *stream) {
     if (cycles < 1 || cycles > (int64_t(1) << 31))
         return set_error(UHS_EINVAL, "cycles must be in [1, 2^31] (got %lld)", static_cast<long long>(cycles));
@@ -1485,6 +1533,13 @@ int uhs_probe_wait_timeout(int64_t cycles, void *stream) {
     cudaError_t e = launch_wait_probe(w, static_cast<long long>(cycles), st);
     if (e != cudaSuccess) return cuda_error(e, "wait probe launch");
     return finish(nullptr, st);
+}
+
+int uhs_probe_dfma_rate(double *per_second, void *stream) {
+    if (!per_second) return set_error(UHS_EINVAL, "per_second is NULL");
+    const cudaError_t e = probe_dfma_rate(per_second, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_error(e, "FP64 rate probe");
+    return UHS_OK;
 }
 
 int uhs_error_norms(const uhs_stencil_desc *d, const uhs_memref *x, const uhs_memref *ref, double out[4],

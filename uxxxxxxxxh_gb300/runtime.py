@@ -128,6 +128,19 @@ def probe_wait_timeout(cycles: int, stream=None) -> int:
     return int(_lib.lib().uhs_probe_wait_timeout(int(cycles), _stream_handle(stream)))
 
 
+def probe_dfma_rate(stream=None) -> float:
+    """FP64 pipe rate of the current device, DFMA per second
+    (uhs_probe_dfma_rate)."""
+    v = ctypes.c_double()
+    _lib.check(_lib.lib().uhs_probe_dfma_rate(ctypes.byref(v), _stream_handle(stream)))
+    return v.value
+
+
+def release_scratch() -> None:
+    """Return the memory kept by the library's scratch pools (uhs_release_scratch)."""
+    _lib.check(_lib.lib().uhs_release_scratch())
+
+
 def error_norms(stencil: Stencil, x, ref, stream=None) -> dict:
     """FP64 error of device grid x against the FP64 device grid ref over the
     stencil's domain, reduced on the GPU (uhs_error_norms)."""
