@@ -97,7 +97,8 @@ def workload_label(st) -> str:
 
 ARITH_LABELS = {1: "fma (IEEE binary64 DFMA for FP64 grids, FFMA for FP32)",
                 2: "exact (separately rounded IEEE products and sums, expression order)",
-                3: "df32 (float pairs: 48-bit significand, FP32 exponent range, on the FP32 pipes)"}
+                3: "df32 (float pairs on the FP32 pipes: 48-bit significand; under AUTO scaled by a power of two "
+                   "chosen per run, so the exponent window is about 2^190 wide anywhere in FP64's range)"}
 
 
 def arith_names_full(code: int) -> str:

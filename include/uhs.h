@@ -56,18 +56,20 @@ enum {
 
 enum {
     UHS_ARITH_AUTO = 0,  /* the backend picks: for F64 grids on the streaming kernel,
-                            UHS_ARITH_DF32 when a device scan of both grids shows
-                            max|x| * (sum|c|)^T < 2^120 and every nonzero |x| >= 2^-50
-                            (one extra read of each grid and one host round trip per
-                            call), else UHS_ARITH_FMA */
+                            float pairs scaled by a power of two chosen from a device
+                            scan of both grids (one extra read of each grid and one
+                            host round trip per call), unless the grids hold Inf/NaN
+                            or span more than about 2^169 between the largest
+                            magnitude grown by (sum|c|)^T and the smallest nonzero
+                            one; then UHS_ARITH_FMA */
     UHS_ARITH_FMA = 1,   /* native arithmetic, products fused into the sum */
     UHS_ARITH_EXACT = 2, /* separately rounded products and sums in expression
                             order: bit-identical to the serial CPU loops */
     UHS_ARITH_DF32 = 3   /* F64 grids computed in float-pair arithmetic on the FP32
-                            pipes: 48-bit significands in the float exponent range (a
-                            value between 2^-74 and 2^128 is held to 2^-48 of itself;
-                            below 2^-74 a pair keeps 24 bits, below 2^-126 it flushes
-                            to zero; 2^128 or more returns UHS_ERANGE) */
+                            pipes, unscaled: 48-bit significands in the float exponent
+                            range (a value between 2^-74 and 2^128 is held to 2^-48 of
+                            itself; below 2^-74 a pair keeps 24 bits, below 2^-126 it
+                            flushes to zero; 2^128 or more returns UHS_ERANGE) */
 };
 
 /* ---- MLIR memref descriptor (rank-3 layout) ---------------------------- */
@@ -184,11 +186,13 @@ int uhs_validate(const uhs_stencil_desc *desc, const uhs_memref *a, const uhs_me
  * allocation fails, or with UHS_FLAG_IN_PLACE, the sweeps run on the FP64
  * grids directly, splitting on every load.
  *
- * Range: UHS_ARITH_AUTO keeps float pairs only when a scan of both grids
- * finds no Inf/NaN, max|x| * (sum|c|)^T below 2^120 and every nonzero |x| at
- * least 2^-50; otherwise the run computes in native FP64.  With either
- * float-pair mode, a value that leaves the float range during the run (2^128
- * or more) makes the call return UHS_ERANGE. */
+ * Range: under UHS_ARITH_AUTO the pairs hold every value times 2^s, with s
+ * chosen from a scan of both grids so that the largest magnitude, grown by
+ * (sum|c|)^T, stays below 2^120 (a linear sweep commutes with the scale
+ * exactly); the run keeps float pairs when every nonzero magnitude, scaled,
+ * is at least 2^-50, and computes in native FP64 otherwise (or when a grid
+ * holds Inf/NaN).  With either float-pair mode, a value that leaves the
+ * float range during the run makes the call return UHS_ERANGE. */
 int uhs_run(const uhs_stencil_desc *desc, const uhs_memref *a, const uhs_memref *b,
             const uhs_params *params, void *stream);
 

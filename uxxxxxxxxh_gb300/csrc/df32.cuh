@@ -15,6 +15,13 @@
 //     low part is dropped and below 2^-126 the value flushes to zero
 //     (absolute error under 2^-74, about 5e-23); 2^128 and above sets the
 //     range flag.
+//   * Scaling: a pair may hold x * 2^s instead of x.  The split then
+//     rebiases the exponent by 896 - s instead of 896 (1023 - 127) and the
+//     join by the same amount back, so the window above applies to x * 2^s:
+//     a run can place any 2^202 range of FP64 magnitudes inside it.  A
+//     linear sweep commutes with the power-of-two scale exactly (every
+//     product and sum of scaled values is the scaled product or sum, as long
+//     as nothing leaves the window), so results do not depend on s.
 //   * df_fma: acc += c * x with the product's rounding error recovered by an
 //     FMA (Dekker/Veltkamp product via fused multiply-add) and the running
 //     sum's by Knuth's TwoSum; error terms are gathered in acc.l.
@@ -33,42 +40,50 @@ struct df {
     float h, l;
 };
 
-__device__ __forceinline__ float2 split_f64(double x, unsigned &range_err) {
+// Exponent rebias between a double x and the float pair of x * 2^shift.
+__host__ __device__ constexpr int pair_bias(int shift) { return 896 - shift; }
+
+// x -> the pair of x * 2^shift (bias = pair_bias(shift)).
+__device__ __forceinline__ float2 split_f64(double x, unsigned &range_err, int bias = 896) {
     const unsigned hi = static_cast<unsigned>(__double2hiint(x)), lo = static_cast<unsigned>(__double2loint(x));
     const unsigned sign = hi & 0x80000000u;
-    const unsigned eb = (hi >> 20) & 0x7ffu;  // biased exponent, E = eb - 1023
-    // h: exponent rebiased by -(1023 - 127) and the top 23 fraction bits
-    // funnel-shifted in from both words.
-    const unsigned f = __funnelshift_l(lo, hi - (896u << 20), 3);
+    // biased float exponent of x * 2^shift (E + 127 + shift, E = eb - 1023)
+    const int fe = static_cast<int>((hi >> 20) & 0x7ffu) - bias;
+    // h: exponent rebiased and the top 23 fraction bits funnel-shifted in
+    // from both words.
+    const unsigned f = __funnelshift_l(lo, hi - (static_cast<unsigned>(bias) << 20), 3);
     const unsigned hb = (f & 0x7fffffffu) | sign;
-    // l: the remaining 29 fraction bits (weight 2^(E-52)), rounded to 24 bits
-    // by the integer-to-float conversion and scaled by 2^(E-52).
+    // l: the remaining 29 fraction bits (weight 2^(fe-127-52)), rounded to 24
+    // bits by the integer-to-float conversion and scaled by that weight.
     const float lm = __uint2float_rn(lo & 0x1fffffffu);
     const float sc = __uint_as_float((hb & 0x7f800000u) - (52u << 23));
     float l = __uint_as_float(__float_as_uint(__fmul_rn(lm, sc)) | sign);
     float h = __uint_as_float(hb);
-    if (eb - 897u >= 254u) {  // E outside [-126, 127]
-        if (eb > 1150u) range_err = 1u;
+    if (static_cast<unsigned>(fe - 1) >= 254u) {  // scaled exponent outside [-126, 127] (or x zero)
+        if (fe > 254) range_err = 1u;
         h = __uint_as_float(sign);
     }
-    if (eb < 1023u - 74u) l = 0.0f;  // 2^(E-52) below the float range: drop the low part
+    if (fe < 53) l = 0.0f;  // the low part's weight below the float range: drop it
     return make_float2(h, l);
 }
 
-// Exact float -> double by bit construction (normal floats and zero; a
-// subnormal float becomes zero).  No FP64 instruction.
-__device__ __forceinline__ double f2d_bits(float v) {
+// Exact float -> double of v * 2^-shift by bit construction (normal floats
+// and zero; a subnormal float becomes zero).  No FP64 instruction.
+__device__ __forceinline__ double f2d_bits(float v, int bias = 896) {
     const unsigned b = __float_as_uint(v);
     const unsigned s = b & 0x80000000u;
-    const unsigned hi = s | (((b & 0x7fffffffu) >> 3) + (896u << 20));
+    const unsigned hi = s | (((b & 0x7fffffffu) >> 3) + (static_cast<unsigned>(bias) << 20));
     const unsigned lo = b << 29;
     return (b & 0x7f800000u) ? __hiloint2double(static_cast<int>(hi), static_cast<int>(lo))
                              : __hiloint2double(static_cast<int>(s), 0);
 }
 
-// (h, l) -> the double nearest h + l: both halves converted exactly, then
-// one correctly rounded FP64 addition (the only FP64 instruction per point).
-__device__ __forceinline__ double join_f64(float h, float l) { return __dadd_rn(f2d_bits(h), f2d_bits(l)); }
+// The pair of x * 2^shift -> the double nearest x = (h + l) * 2^-shift: both
+// halves converted exactly, then one correctly rounded FP64 addition (the
+// only FP64 instruction per point).
+__device__ __forceinline__ double join_f64(float h, float l, int bias = 896) {
+    return __dadd_rn(f2d_bits(h, bias), f2d_bits(l, bias));
+}
 
 // acc = c * x  (first term)
 __device__ __forceinline__ void df_mul(df &acc, float ch, float cl, float2 x) {

@@ -1,4 +1,6 @@
 // FP64 grid <-> float-pair grid conversion for pair-resident runs.
+// The pairs may hold the values scaled by a power of two (df32.cuh): the
+// split applies the run's scale and the join removes it.
 //
 // A program of T >= 8 float-pair sweeps on FP64 grids (a star of radius 1-2
 // or a separable box; pair_eligible in uhs_runtime.cpp) runs on float-pair
@@ -24,6 +26,7 @@ struct PairConv {
     int64_t n0, n1, n2;          // grid sizes
     int64_t lb0, lb1, lb2, ub0, ub1, ub2;
     int halo_only;  // to pairs: convert only cells outside [lb, ub)
+    int bias;       // exponent rebias of the pairs: they hold x * 2^shift (pair_bias, df32.cuh)
     unsigned *err;
 };
 
@@ -44,11 +47,11 @@ __global__ void __launch_bounds__(kConvThreads) k_to_pairs(const PairConv a) {
             const int64_t left = a.lb2, right = a.n2 - a.ub2;
             for (int64_t i = lane; i < left + right; i += 32) {
                 const int64_t x = i < left ? i : a.ub2 + (i - left);
-                d[x] = split_f64(s[x], rerr);
+                d[x] = split_f64(s[x], rerr, a.bias);
             }
         } else {
 #pragma unroll 4
-            for (int64_t x = lane; x < a.n2; x += 32) d[x] = split_f64(s[x], rerr);
+            for (int64_t x = lane; x < a.n2; x += 32) d[x] = split_f64(s[x], rerr, a.bias);
         }
     }
     if (rerr) atomicOr(a.err, kDevErrRange);
@@ -71,7 +74,7 @@ __global__ void __launch_bounds__(kConvThreads) k_from_pairs(const PairConv a) {
         for (int64_t x = a.lb2 + lane; x < a.ub2; x += 32) {
             const float2 v = s[x];
             rerr |= (__float_as_uint(v.x) & 0x7f800000u) == 0x7f800000u;
-            d[x] = join_f64(v.x, v.y);
+            d[x] = join_f64(v.x, v.y, a.bias);
         }
     }
     if (rerr) atomicOr(a.err, kDevErrRange);
@@ -88,9 +91,9 @@ unsigned conv_blocks(int64_t rows) {
 }  // namespace
 
 cudaError_t launch_to_pairs(const GridView &src, const GridView &dst, const int64_t lb[3], const int64_t ub[3],
-                            bool halo_only, unsigned *err, cudaStream_t st) {
+                            bool halo_only, int shift, unsigned *err, cudaStream_t st) {
     PairConv a{src.data, dst.data, src.s[0], src.s[1], dst.s[0], dst.s[1], src.n[0], src.n[1], src.n[2],
-               lb[0], lb[1], lb[2], ub[0], ub[1], ub[2], halo_only ? 1 : 0, err};
+               lb[0], lb[1], lb[2], ub[0], ub[1], ub[2], halo_only ? 1 : 0, pair_bias(shift), err};
     if (src.n[0] * src.n[1] <= 0 || src.n[2] <= 0) return cudaSuccess;
     k_to_pairs<<<conv_blocks(src.n[0] * src.n[1]), kConvThreads, 0, st>>>(a);
     count_launch();
@@ -98,9 +101,9 @@ cudaError_t launch_to_pairs(const GridView &src, const GridView &dst, const int6
 }
 
 cudaError_t launch_from_pairs(const GridView &src, const GridView &dst, const int64_t lb[3], const int64_t ub[3],
-                              unsigned *err, cudaStream_t st) {
+                              int shift, unsigned *err, cudaStream_t st) {
     PairConv a{src.data, dst.data, src.s[0], src.s[1], dst.s[0], dst.s[1], src.n[0], src.n[1], src.n[2],
-               lb[0], lb[1], lb[2], ub[0], ub[1], ub[2], 0, err};
+               lb[0], lb[1], lb[2], ub[0], ub[1], ub[2], 0, pair_bias(shift), err};
     const int64_t rows = (ub[0] - lb[0]) * (ub[1] - lb[1]);
     if (rows <= 0 || ub[2] <= lb[2]) return cudaSuccess;
     k_from_pairs<<<conv_blocks(rows), kConvThreads, 0, st>>>(a);

@@ -192,6 +192,7 @@ void batch_fill_args(BatchArgs *a, const StreamCall &c, int nt) {
     a->zchunk = c.zchunk;
     a->shift = 0;
     a->pair_loads = c.pair_loads;
+    a->pair_shift = c.pair_shift;
     a->err = c.err;
     fill_coefs(a->cd, a->chl, a->cl_sum, c.coef, nt < kBatchNT ? nt : kBatchNT, c.shape, c.R);
 }

@@ -32,6 +32,7 @@ struct StreamArgs {
     int zchunk;
     int shift;       // TMA box starts this many elements left of x0 - R (16-byte granule)
     int pair_loads;  // cp.async of 4-byte elements in 8-byte pairs (origin and pitches even)
+    int pair_shift;  // FP64 grids in float pairs: the pairs hold x * 2^pair_shift (df32.cuh)
     unsigned *err;
     double cd[NT];
     float2 chl[NT];  // float rounding of each coefficient and its rounding error (hi, lo)
@@ -66,6 +67,7 @@ struct StreamCall {
     const CUtensorMap *tmap;
     int shift;
     int pair_loads;
+    int pair_shift;  // FP64 grids in float pairs: power-of-two scale of the pairs (0: none)
     unsigned *err;
     cudaStream_t stream;
     int *occ_out;  // when set: report CTAs per SM of the variant instead of launching

@@ -45,6 +45,7 @@ struct FusedArgs {
     int64_t n0, n1, n2;
     int64_t lb0, lb1, lb2, ub0, ub1, ub2;
     int zchunk;
+    int pair_shift;  // FP64 grids in float pairs: the pairs hold x * 2^pair_shift (df32.cuh)
     unsigned *err;
     double cd[7];
     float2 chl[7];
@@ -68,7 +69,7 @@ struct FArith<C, kArNative> {  // float grids: centre correction as in Arith (st
         if constexpr (F32) s = fmaf(a.cl_sum, v, s);
     }
     __device__ static T level(const Acc &s) { return s; }
-    __device__ static void store(T *p, const Acc &s, unsigned &) { *p = s; }
+    __device__ static void store(T *p, const Acc &s, unsigned &, int) { *p = s; }
 };
 template <class C>
 struct FArith<C, kArDf32> {
@@ -79,10 +80,11 @@ struct FArith<C, kArDf32> {
     __device__ static void add(Acc &s, const FusedArgs &a, int k, float2 v) { df_fma(s, a.chl[k].x, a.chl[k].y, v); }
     __device__ static void centre(Acc &, const FusedArgs &, float2) {}
     __device__ static float2 level(const Acc &s) { return renorm(s); }
-    // a sum that outgrew the float range sets the range flag (as in Arith)
-    __device__ static void store(double *p, const Acc &s, unsigned &range_err) {
+    // joined with the run's exponent bias; a sum that outgrew the float range
+    // sets the range flag (as in Arith)
+    __device__ static void store(double *p, const Acc &s, unsigned &range_err, int bias) {
         range_err |= (__float_as_uint(s.h) & 0x7f800000u) == 0x7f800000u;
-        *p = join_f64(s.h, s.l);
+        *p = join_f64(s.h, s.l, bias);
     }
 };
 
@@ -140,7 +142,7 @@ __global__ void __launch_bounds__(256) k_fused(const __grid_constant__ FusedArgs
         if constexpr (C::CONVERT) {
             const double *sp = reinterpret_cast<const double *>(stg + (i % NSTG) * PLANE);
             float2 *dp = lvl0 + (i % 3) * PLANE;
-            for (int e = tid; e < PLANE; e += 256) dp[e] = split_f64(sp[e], range_err);
+            for (int e = tid; e < PLANE; e += 256) dp[e] = split_f64(sp[e], range_err, pair_bias(a.pair_shift));
             __syncthreads();
         }
 #pragma unroll
@@ -172,7 +174,8 @@ __global__ void __launch_bounds__(256) k_fused(const __grid_constant__ FusedArgs
                     else v = lv(j - 1, sp_, e);
                     rings[((j - 1) * 3 + sp_ % 3) * PLANE + e] = v;
                 } else if (in_dom) {
-                    A::store(static_cast<TS *>(a.out) + p * a.out_s0 + gy * a.out_s1 + gx, acc, range_err);
+                    A::store(static_cast<TS *>(a.out) + p * a.out_s0 + gy * a.out_s1 + gx, acc, range_err,
+                             pair_bias(a.pair_shift));
                 }
             }
             __syncthreads();
@@ -226,6 +229,7 @@ cudaError_t launch_fused_t(const StreamCall &c) {
     a.ub1 = c.ub[1];
     a.ub2 = c.ub[2];
     a.zchunk = c.zchunk;
+    a.pair_shift = c.pair_shift;
     a.err = c.err;
     float sums[3];
     fill_coefs(a.cd, a.chl, sums, c.coef, 7, c.shape, c.R);

@@ -224,7 +224,7 @@ struct Arith<C, kArNative> {
     __device__ static __forceinline__ void centre(Acc &acc, const Args &a, int pass, TS v) {
         if constexpr (F32) acc = fmaf(a.cl_sum[pass], v, acc);
     }
-    __device__ static __forceinline__ void store(TS *p, const Acc &acc, unsigned &) { *p = acc; }
+    __device__ static __forceinline__ void store(TS *p, const Acc &acc, unsigned &, int) { *p = acc; }
     __device__ static __forceinline__ TS level(const Acc &acc) { return acc; }
 };
 
@@ -241,13 +241,14 @@ struct Arith<C, kArDf32> {
         const float2 c = coef_f2<C>(a, k);
         df_fma(acc, c.x, c.y, v);
     }
-    // FP64 grids: a sum that outgrew the float range (hi Inf or NaN) would
-    // join to a finite double near 2^128; it sets the range flag instead of
+    // FP64 grids: joined back with the run's exponent bias (the pairs hold
+    // x * 2^pair_shift).  A sum that outgrew the float range (hi Inf or NaN)
+    // would join to a finite double; it sets the range flag instead of
     // passing unnoticed.
-    __device__ static __forceinline__ void store(typename C::TS *p, const Acc &acc, unsigned &range_err) {
+    __device__ static __forceinline__ void store(typename C::TS *p, const Acc &acc, unsigned &range_err, int bias) {
         if constexpr (C::ST == kStF64) {
             range_err |= (__float_as_uint(acc.h) & 0x7f800000u) == 0x7f800000u;
-            *p = join_f64(acc.h, acc.l);
+            *p = join_f64(acc.h, acc.l, bias);
         } else {
             *p = renorm(acc);
         }
@@ -450,7 +451,8 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                 if (r < H) {
 #pragma unroll
                     for (int c0 = 0; c0 < WL; c0 += BX)
-                        if (c0 + tx < WL) dp[r * W + c0 + tx] = split_f64(sp[r * W + c0 + tx], range_err);
+                        if (c0 + tx < WL)
+                            dp[r * W + c0 + tx] = split_f64(sp[r * W + c0 + tx], range_err, pair_bias(a.pair_shift));
                 }
             }
             __syncthreads();
@@ -580,7 +582,7 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
             }
 #pragma unroll
             for (int v = 0; v < VY; ++v)
-                if (v < vmax) A::store(optr + v * a.out_s1, acc[v], range_err);
+                if (v < vmax) A::store(optr + v * a.out_s1, acc[v], range_err, pair_bias(a.pair_shift));
             optr += a.out_s0;
         }
         // advance the rings

@@ -32,6 +32,7 @@ cudaError_t launch_cfg(const StreamCall &c) {
     a.zchunk = c.zchunk;
     a.shift = c.shift;
     a.pair_loads = c.pair_loads;
+    a.pair_shift = c.pair_shift;
     a.err = c.err;
     fill_coefs(a.cd, a.chl, a.cl_sum, c.coef, C::NT, c.shape, c.R);
     const int64_t nz = c.ub[0] - c.lb[0], ny = c.ub[1] - c.lb[1], nx = c.ub[2] - c.lb[2];

@@ -92,12 +92,13 @@ cudaError_t launch_error_norms(const ErrNormsCall &c);
 // Pair-resident runs (pairs.cu): an FP64 grid's values split into a
 // contiguous float-pair grid (the whole grid, or only the cells outside the
 // domain [lb, ub)), and the domain of a float-pair grid joined back.
+// The pairs hold the values times 2^shift (the run's scale, df32.cuh).
 cudaError_t launch_to_pairs(const GridView &src, const GridView &dst, const int64_t lb[3], const int64_t ub[3],
-                            bool halo_only, unsigned *err, cudaStream_t st);
+                            bool halo_only, int shift, unsigned *err, cudaStream_t st);
 // The join sets kDevErrRange in *err when a pair holds Inf or NaN (a value
 // that outgrew the float range during the sweeps).
 cudaError_t launch_from_pairs(const GridView &src, const GridView &dst, const int64_t lb[3], const int64_t ub[3],
-                              unsigned *err, cudaStream_t st);
+                              int shift, unsigned *err, cudaStream_t st);
 
 // Exponent range of n_words doubles: the largest biased exponent field into
 // *max_out (atomicMax; must start at 0) and the smallest biased exponent field

@@ -209,6 +209,7 @@ struct Plan {
     int pd = 0;                // planes (rows) the streaming kernel loads ahead: built into its variant
     std::vector<double> coef;  // coef_slot order
     bool auto_df32 = false;    // df32 chosen by UHS_ARITH_AUTO, subject to range_ok()
+    int pair_shift = 0;        // FP64 grids in float pairs: the pairs hold x * 2^pair_shift (range_ok)
     bool factored = false;     // separable box run as 1D passes
     bool a_tmem = false;       // tensor-core path: A operand staged in tensor memory
 };
@@ -594,22 +595,26 @@ static GridView kernel_view(const SweepSpec &sp, const GridView &v) {
     return k;
 }
 
-// UHS_ARITH_AUTO on FP64 grids: a float pair holds a value to 2^-48 of
-// itself between 2^-74 and 2^128 (df32.cuh).  Scan both grids (their whole
+// UHS_ARITH_AUTO on FP64 grids.  A float pair holds a value to 2^-48 of
+// itself between 2^-74 and 2^128 (df32.cuh), and a run may keep every value
+// scaled by 2^s, which moves that window anywhere in the FP64 range (a linear
+// sweep commutes with the scale exactly).  Scan both grids (their whole
 // spans, halo included) for their exponent range and keep float pairs only
 // when
 //   * no cell holds Inf or NaN;
-//   * the largest magnitude grown by (sum |c|)^T over the run stays below
-//     2^120 (8 binades under the float range);
-//   * every nonzero magnitude is at least 2^kPairMinExp, 24 binades above
-//     2^-74, so every input value is split exactly to 48 bits and values the
-//     run brings down by up to 2^24 still are.
-// Otherwise the run computes in native FP64.  Below 2^-74 a pair keeps 24
-// significant bits and below 2^-126 it flushes to zero, so without the
-// second bound a field spanning 1 ... 1e-30 would lose precision in its small
-// cells while a max-normalised error would not show it.
-constexpr int kPairMinExp = -50;
-static bool range_ok(const SweepSpec &sp, const GridView &a, const GridView &b, int T, cudaStream_t st) {
+//   * with s chosen so that the largest magnitude grown by (sum |c|)^T over
+//     the run stays below 2^120 (8 binades under the float range), every
+//     nonzero magnitude, scaled, is at least 2^(-74 + kPairLowMargin): each
+//     input value splits exactly to 48 bits, and values the run brings down
+//     by up to 2^kPairLowMargin still do.
+// Otherwise the run computes in native FP64.  A field spanning more than
+// about 2^169 between its largest (grown) and smallest nonzero magnitudes is
+// the case left to native arithmetic: in float pairs its small cells would
+// keep 24 bits or flush to zero, which a max-normalised error would not show.
+constexpr int kPairLowMargin = 24;
+static bool range_ok(const SweepSpec &sp, const GridView &a, const GridView &b, int T, cudaStream_t st,
+                     int *shift) {
+    *shift = 0;
     int dev = 0;
     cudaGetDevice(&dev);
     unsigned *w = stream_error_word(dev, st);
@@ -626,12 +631,20 @@ static bool range_ok(const SweepSpec &sp, const GridView &a, const GridView &b, 
     if (cudaMemcpyAsync(&e[1], emin, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess) return false;
     if (cudaStreamSynchronize(st) != cudaSuccess) return false;
     if (e[0] >= 0x7ffu) return false;  // Inf or NaN somewhere
-    // all cells zero: e[1] stays 0xffffffff, which passes
-    if (e[1] != 0xffffffffu && static_cast<int>(e[1]) - 1023 < kPairMinExp) return false;
+    if (e[1] == 0xffffffffu) return true;  // every cell zero
     double csum = 0.0;
     for (int k = 0; k < sp.nterms; ++k) csum += std::fabs(sp.coef[k]);
     const double growth = csum > 1.0 ? std::max(T, 1) * std::log2(csum) : 0.0;
-    return static_cast<double>(static_cast<int>(e[0]) - 1023) + 1.0 + growth < 120.0;
+    // log2 bound of every magnitude during the run, and the largest scale
+    // that keeps it below 2^120 (kept within +-800 so scaled exponents and
+    // their joins stay inside the FP64 range)
+    const double top = static_cast<double>(static_cast<int>(e[0]) - 1023) + 1.0 + growth;
+    const double sd = std::floor(119.0 - top);
+    if (!(sd >= -800.0)) return false;
+    const int sh = static_cast<int>(std::min(sd, 800.0));
+    if (static_cast<int>(e[1]) - 1023 + sh < -74 + kPairLowMargin) return false;
+    *shift = sh;
+    return true;
 }
 
 static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in, const GridView &out,
@@ -683,6 +696,7 @@ static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in,
     int dev = 0;
     cudaGetDevice(&dev);
     c.err = err_word ? err_word : stream_error_word(dev, st);
+    c.pair_shift = pl.pair_shift;
     if (!c.err) return set_error(UHS_ENOMEM, "device error word allocation failed");
     const int eb = sp.dtype == UHS_F32 ? 4 : 8;
     CUtensorMap tmap;
@@ -794,6 +808,7 @@ static int launch_fused_pass(const SweepSpec &sp, const Plan &pl, const GridView
     cudaGetDevice(&dev);
     c.err = stream_error_word(dev, st);
     if (!c.err) return set_error(UHS_ENOMEM, "device error word allocation failed");
+    c.pair_shift = pl.pair_shift;
     const int64_t nz = sp.ub[0] - sp.lb[0];
     const int64_t tiles = ((sp.ub[2] - sp.lb[2] + 31) / 32) * ((sp.ub[1] - sp.lb[1] + 15) / 16);
     int zchunk = pl.cfg.tile_z;
@@ -1042,7 +1057,8 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
             }
             if (pl.kernel != UHS_KERNEL_STREAM)
                 return set_error(UHS_EUNSUPPORTED, "program %d is not a star/box stencil the batched kernel covers", i);
-            if (pl.auto_df32 && descs[i].iterations > 0 && !range_ok(sp, va, vb, descs[i].iterations, scan_stream)) {
+            if (pl.auto_df32 && descs[i].iterations > 0 &&
+                !range_ok(sp, va, vb, descs[i].iterations, scan_stream, &pl.pair_shift)) {
                 pl.ar = kArNative;
                 pl.cfg.arith = UHS_ARITH_FMA;
             }
@@ -1084,7 +1100,8 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
         if ((rc = plan_sweep(sp, &bp, va, &pl))) return set_error(rc, "program %d: %s", i, uhs_last_error());
         if (pl.kernel != UHS_KERNEL_STREAM)
             return set_error(UHS_EUNSUPPORTED, "program %d is not a star/box stencil the batched kernel covers", i);
-        if (pl.auto_df32 && descs[i].iterations > 0 && !range_ok(sp, va, vb, descs[i].iterations, scan_stream)) {
+        if (pl.auto_df32 && descs[i].iterations > 0 &&
+            !range_ok(sp, va, vb, descs[i].iterations, scan_stream, &pl.pair_shift)) {
             pl.ar = kArNative;
             pl.cfg.arith = UHS_ARITH_FMA;
         }
@@ -1109,6 +1126,7 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
         c.lb[2] = sp.lb[2];
         c.ub[2] = sp.ub[2];
         c.err = err;
+        c.pair_shift = pl.pair_shift;
         int bx, by, zc;
         batch_tile(pl.shape, pl.R, pl.st, &bx, &by, &zc);
         const int eb = sp.dtype == UHS_F32 ? 4 : 8;
@@ -1270,8 +1288,9 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
                 for (int gi : branch[k]) {
                     const BatchSolo &g = solo[gi];
                     if (g.pairs) {  // split a, and b's halo, into the copies
-                        e = launch_to_pairs(g.va, g.pa, g.sp.lb, g.sp.ub, false, err, bs_[k]);
-                        if (e == cudaSuccess) e = launch_to_pairs(g.vb, g.pb, g.sp.lb, g.sp.ub, true, err, bs_[k]);
+                        const int sh = g.pl.pair_shift;
+                        e = launch_to_pairs(g.va, g.pa, g.sp.lb, g.sp.ub, false, sh, err, bs_[k]);
+                        if (e == cudaSuccess) e = launch_to_pairs(g.vb, g.pb, g.sp.lb, g.sp.ub, true, sh, err, bs_[k]);
                         launches += 2;
                         if (e != cudaSuccess) break;
                     }
@@ -1286,8 +1305,9 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
                     }
                     if (rc) break;
                     if (g.pairs) {  // both domains back (T >= 8 sweeps wrote both grids)
-                        e = launch_from_pairs(g.pa, g.va, g.sp.lb, g.sp.ub, err, bs_[k]);
-                        if (e == cudaSuccess) e = launch_from_pairs(g.pb, g.vb, g.sp.lb, g.sp.ub, err, bs_[k]);
+                        const int sh = g.pl.pair_shift;
+                        e = launch_from_pairs(g.pa, g.va, g.sp.lb, g.sp.ub, sh, err, bs_[k]);
+                        if (e == cudaSuccess) e = launch_from_pairs(g.pb, g.vb, g.sp.lb, g.sp.ub, sh, err, bs_[k]);
                         launches += 2;
                         if (e != cudaSuccess) break;
                     }
@@ -1447,7 +1467,7 @@ static cudaError_t dev_alloc_async(void **p, size_t bytes, cudaStream_t st) {
 // *ran stays false when the scratch could not be had or planned, and the
 // caller then sweeps the FP64 grids in place.
 static int run_pair_resident(const SweepSpec &sp, const uhs_params *p, const GridView &va, const GridView &vb,
-                             int T, cudaStream_t st, bool *ran) {
+                             int T, int shift, cudaStream_t st, bool *ran) {
     *ran = false;
     int dev = 0;
     cudaGetDevice(&dev);
@@ -1480,16 +1500,16 @@ static int run_pair_resident(const SweepSpec &sp, const uhs_params *p, const Gri
     }
     *ran = true;
     int rc = UHS_OK;
-    cudaError_t e = launch_to_pairs(va, pa, sp.lb, sp.ub, false, err, st);
-    if (e == cudaSuccess) e = launch_to_pairs(vb, pb, sp.lb, sp.ub, true, err, st);
+    cudaError_t e = launch_to_pairs(va, pa, sp.lb, sp.ub, false, shift, err, st);
+    if (e == cudaSuccess) e = launch_to_pairs(vb, pb, sp.lb, sp.ub, true, shift, err, st);
     if (e != cudaSuccess) rc = cuda_error(e, "float-pair conversion");
     for (int it = 0; it < T / 2 && rc == UHS_OK; ++it) {
         if ((rc = launch_sweep(sp2, pl2, pa, pb, st))) break;
         rc = launch_sweep(sp2, pl2, pb, pa, st);
     }
     if (rc == UHS_OK) {
-        e = launch_from_pairs(pa, va, sp.lb, sp.ub, err, st);
-        if (e == cudaSuccess) e = launch_from_pairs(pb, vb, sp.lb, sp.ub, err, st);
+        e = launch_from_pairs(pa, va, sp.lb, sp.ub, shift, err, st);
+        if (e == cudaSuccess) e = launch_from_pairs(pb, vb, sp.lb, sp.ub, shift, err, st);
         if (e != cudaSuccess) rc = cuda_error(e, "float-pair conversion");
     }
     cudaFreeAsync(buf, st);
@@ -1665,7 +1685,7 @@ int uhs_sweep(const uhs_stencil_desc *d, const uhs_memref *in, const uhs_memref 
     Plan pl;
     if ((rc = plan_sweep(sp, p, vi, &pl))) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (pl.auto_df32 && !range_ok(sp, vi, vo, 1, st)) {
+    if (pl.auto_df32 && !range_ok(sp, vi, vo, 1, st, &pl.pair_shift)) {
         pl.ar = kArNative;
         pl.cfg.arith = UHS_ARITH_FMA;
     }
@@ -1685,7 +1705,7 @@ int uhs_run(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_memref *b,
     Plan pl;
     if ((rc = plan_sweep(sp, p, va, &pl))) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (pl.auto_df32 && d->iterations > 0 && !range_ok(sp, va, vb, d->iterations, st)) {
+    if (pl.auto_df32 && d->iterations > 0 && !range_ok(sp, va, vb, d->iterations, st, &pl.pair_shift)) {
         pl.ar = kArNative;
         pl.cfg.arith = UHS_ARITH_FMA;
     }
@@ -1707,7 +1727,7 @@ int uhs_run(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_memref *b,
     }
     if (pair_eligible(pl, d->iterations, p)) {
         bool ran = false;
-        rc = run_pair_resident(sp, p, va, vb, d->iterations, st, &ran);
+        rc = run_pair_resident(sp, p, va, vb, d->iterations, pl.pair_shift, st, &ran);
         if (ran) return rc ? rc : finish(p, st);
     }
     if (d->iterations == 1) {
