@@ -13,9 +13,18 @@ Writes
                            a few sample cells.  Each digest is written only
                            after the oracle's result was checked bit-for-bit
                            against the reference's result in this run.
+  fusion_pins.json         the spatially fused program laplaceAddInput
+                           (test/Examples/StencilDialect/laplaceAddInputIteration:
+                           a producer kernel inlined into its consumer) as the
+                           DSL reader reads it, and the SHA-256 of the grid its
+                           driver's serial loop leaves (run as an executable,
+                           grid read from the mpe_result file it writes),
+                           written after the oracle reproduced it bit-for-bit.
 UH-SW cases run mpe_verify (T = 20 on 4096^2 / 256^3).  UH-SW/3d3r_box's
 mpe_verify jumps past its loops (stencil_3d343pt_driver.serial.c:43), so the
 343-point box is pinned through UH-GPU/3d3r_box's cpu_verify (T = 4 on 512^3).
+
+  python tests/golden/make_golden.py [REFERENCE_ROOT] [--fusion-only]
 """
 from __future__ import annotations
 
@@ -62,6 +71,26 @@ def samples(a: np.ndarray, st: uhs.Stencil) -> list:
     return out
 
 
+def fusion(ref_root: str) -> None:
+    import tempfile
+    from oracle import build_ref
+    st = uhs.parse_dsl_file(os.path.join(ref_root, build_ref.FUSION_DSL))
+    n = int(np.prod(st.sizes))
+    a, b = np.empty(n), np.empty(n)
+    oracle.fill_rand50([a, b])  # the driver fills input and output alike
+    oracle.iterate_f64(st, a, b)
+    with tempfile.TemporaryDirectory() as d:
+        ref = np.array(build_ref.run_fusion_driver(d))
+    same = np.array_equal(ref.view(np.uint64), a.view(np.uint64))
+    print(f"fusion laplaceAddInput: bit-exact={same}", flush=True)
+    if not same:
+        raise SystemExit("oracle differs from the reference on the fused program")
+    rec = {"program": stencil_record(st, build_ref.FUSION_DSL), "driver": build_ref.FUSION[1], "cells": n,
+           "iterations": st.iterations, "sha256": digest(a), "samples": samples(a, st)}
+    with open(os.path.join(HERE, "fusion_pins.json"), "w") as f:
+        json.dump(rec, f, indent=1)
+
+
 def main(ref_root: str) -> None:
     stencils = {}
     for kind, sub in (("sw", "UH-SW"), ("gpu", "UH-GPU")):
@@ -95,11 +124,16 @@ def main(ref_root: str) -> None:
                       "sha256": digest(a), "samples": samples(a, st)}
     with open(os.path.join(HERE, "reference_pins.json"), "w") as f:
         json.dump(pins, f, indent=1)
+    fusion(ref_root)
 
 
 if __name__ == "__main__":
     from oracle.build_ref import reference_root
-    root = sys.argv[1] if len(sys.argv) > 1 else reference_root()
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    root = args[0] if args else reference_root()
     if not root:
         raise SystemExit("reference checkout not found (pass its path or set UHS_REFERENCE_ROOT)")
-    main(root)
+    if "--fusion-only" in sys.argv:
+        fusion(root)
+    else:
+        main(root)

@@ -204,3 +204,23 @@ def _program(text):
     prog = ctypes.c_void_p()
     _lib.check(_lib.lib().uhs_dsl_parse(text.encode(), b"t.dsl", ctypes.byref(prog)))
     return prog
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference checkout not present")
+def test_reader_fuses_the_reference_producer_consumer_program():
+    """laplaceAddInputIteration.dsl has two kernels: laplace (a 5-point
+    expression over the two slowest axes) and addInput, which reads laplace at
+    the same point.  The reader inlines the producer into the consumer -- the
+    reference's kernel-fusion pass (lib/Dialect/Stencil/StencilKernelFusion.cpp:
+    70-183) -- giving one sweep with the recorded term list.  The domain
+    covers the fastest axis whole ([0, 16), no halo on it)."""
+    from oracle.build_ref import FUSION_DSL
+    rec = json.load(open(os.path.join(HERE, "golden", "fusion_pins.json")))["program"]
+    st = uhs.parse_dsl_file(os.path.join(REF, FUSION_DSL))
+    assert st.name == rec["name"] and list(st.sizes) == rec["sizes"]
+    assert list(st.lb) == rec["lb"] and list(st.ub) == rec["ub"] and st.iterations == rec["iterations"]
+    assert [list(t) for t in st.terms] == rec["terms"]
+    assert st.lb[2] == 0 and st.ub[2] == st.sizes[2]
+    # consumer's own access first, then the inlined producer's five terms;
+    # the consumer adds a subtree, so the linear form is not a left-deep sum
+    assert st.terms[0][:3] == (0, 0, 0) and len(st.terms) == 6 and not st.exact_order

@@ -6,11 +6,14 @@ must reproduce its grid bit-for-bit.  Everywhere, the oracle's result must
 hash to the digest tests/golden/make_golden.py recorded from that comparison.
 """
 import hashlib
+import os
+import tempfile
 
 import numpy as np
 import pytest
 
 import oracle
+import uxxxxxxxxh_gb300 as uhs
 from golden_util import load, reference_stencil
 
 PINS = load("reference_pins.json")
@@ -46,6 +49,37 @@ def test_oracle_matches_343pt_box_digest():
     (512^3, T = 4); its digest was recorded after a bit-exact comparison."""
     st, a = _oracle_run("3d3r_box", "gpu")
     assert hashlib.sha256(a.tobytes()).hexdigest() == PINS["3d3r_box"]["sha256"]
+
+
+def fusion_program():
+    rec = load("fusion_pins.json")["program"]
+    return uhs.Stencil(name=rec["name"], rank=rec["rank"], sizes=tuple(rec["sizes"]), lb=tuple(rec["lb"]),
+                       ub=tuple(rec["ub"]), terms=[tuple(t) for t in rec["terms"]], iterations=rec["iterations"],
+                       exact_order=rec["exact_order"])
+
+
+def test_oracle_matches_fused_reference_program():
+    """Spatial kernel fusion: the program laplaceAddInput inlines its producer
+    kernel (laplace) into its consumer (addInput), as the reference's
+    kernel-fusion pass does (lib/Dialect/Stencil/StencilKernelFusion.cpp:
+    70-183).  The DSL reader's fused term list, run by the oracle on the
+    driver's own rand() % 50 data, reproduces the grid the driver's serial
+    loop leaves (laplaceAddInputIteration_driver.c:37-58): through the
+    recorded digest everywhere, and bit-for-bit against the driver itself
+    where oracle/_ref holds it."""
+    pin = load("fusion_pins.json")
+    st = fusion_program()
+    n = int(np.prod(st.sizes))
+    a, b = np.empty(n), np.empty(n)
+    oracle.fill_rand50([a, b])
+    oracle.iterate_f64(st, a, b)
+    assert hashlib.sha256(a.tobytes()).hexdigest() == pin["sha256"]
+    exe = os.path.join(oracle.REF_DIR, "fusion_laplaceAddInputIteration")
+    if os.path.exists(exe):
+        from oracle.build_ref import run_fusion_driver
+        with tempfile.TemporaryDirectory() as d:
+            ref = np.array(run_fusion_driver(d))
+        assert np.array_equal(ref.view(np.uint64), a.view(np.uint64))
 
 
 def test_oracle_rejects_odd_iteration_counts():
