@@ -78,8 +78,14 @@ def parse_args():
 # interior points.  Keyed by (shape, grid element type the kernel sweeps,
 # arithmetic).
 NCU_BYTES_PER_POINT = {
-    ("3d1r_star", "f64", "df32"): 15.10, ("3d1r_star", "f64", "fma"): 15.20, ("3d1r_star", "f32", "fma"): 6.77,
-    ("3d1r_star", "f32x2", "df32"): 15.00,
+    # FP64 grids swept in place (320^3)
+    ("3d1r_star", "f64", "df32"): 15.10, ("3d1r_star", "f64", "fma"): 15.20,
+    # the sweeps of pair-resident runs (float-pair grids) and FP32 grids:
+    # profiles/traffic_sweeps_small_cases.md
+    ("3d1r_star", "f32x2", "df32"): 15.34, ("3d1r_star", "f32", "fma"): 6.78,
+    ("3d2r_star", "f32x2", "df32"): 15.97, ("3d2r_star", "f32", "fma"): 6.91,
+    ("3d3r_box_sep", "f32x2", "df32"): 16.08, ("3d3r_box_sep", "f32", "fma"): 7.11,
+    ("2d1r_star", "f32x2", "df32"): 15.59, ("2d1r_star", "f32", "fma"): 7.35,
 }
 
 
@@ -776,7 +782,8 @@ def main():
         "config": {"workload": workload_label(st),
                    "parallelism": "replicas" if world > 1 else "1 GPU", "l2": "inputs larger than L2 (no flush)",
                    "kernel": plan.kernel, "arith": arith_names.get(plan.arith, plan.arith),
-                   "tile": [plan.tile_x, plan.tile_y, plan.tile_z], "k_temporal": plan.k_temporal,
+                   "tile": ([plan_k.tile_x, plan_k.tile_y, plan_k.tile_z, plan_k.vy] if pair_resident else
+                            [plan.tile_x, plan.tile_y, plan.tile_z, plan.vy]), "k_temporal": plan.k_temporal,
                    "pair_resident": pair_resident},
         "pct_hbm_roofline": achieved / peak,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -32,7 +32,15 @@ def test_float_pair_stars(r, want):
     assert planned(st) == want
 
 
-@pytest.mark.parametrize("r,want", [(1, (32, 32, 4)), (2, (32, 16, 4)), (3, (32, 32, 4))])
+@pytest.mark.parametrize("r", [1, 2, 3])
+def test_float_pair_grid_stars(r):
+    """Float-pair grids (the sweeps of pair-resident runs) take 32 x 16 tiles
+    of 4 points per thread for every radius."""
+    st, _ = random_case(3, r, "star", (64, 64, 64), 2, 1, dtype=F.UHS_F32X2)
+    assert planned(st) == (32, 16, 4)
+
+
+@pytest.mark.parametrize("r,want", [(1, (32, 16, 4)), (2, (32, 16, 4)), (3, (32, 16, 4))])
 def test_float_pair_separable_boxes(r, want):
     st = separable_box(r, F.UHS_F64)
     assert plan(st, memref_raw(1 << 20, st.sizes), params=NO_DB).factored == 1

@@ -94,6 +94,17 @@ struct StreamCfg {
     static constexpr int SMEM = NSTG * STG_SLOT + (CONVERT ? NCMP * CMP_SLOT : 0) + NSTG * 8;
     static constexpr int THREADS = BX * TYT;
     static constexpr int NT = SI::NT;
+    // 3D sweeps in float-pair arithmetic sum a thread's points two rows at a
+    // time in packed FP32 instructions (df2_*_s, df32.cuh) in standalone
+    // launches.  GB300 at 512^3 (256^3 for radius 2-3 boxes), GStencil/s per
+    // sweep, scalar -> packed: stars on float-pair grids r1/r2/r3 330/184/129
+    // -> 341/186/134 (best tiles), on FP64 grids 169/114/86 -> 191/130/97;
+    // separable boxes FP64 141/92/63 -> 163/102/68; radius-3 boxes 5.5/6.0 ->
+    // 7.5/7.2.  Term-by-term boxes of radius 1 on float-pair grids (100 ->
+    // 96) and of radius 2 (21.2 -> 20.4, FP64 19.3 -> 19.0) keep the scalar
+    // sums.
+    static constexpr bool PACKED = AR == kArDf32 && !SI::is2d && VY % 2 == 0 &&
+                                   !(SHAPE == kBox3 && (R == 2 || (R == 1 && ST == kStF32x2)));
     static_assert(LD != kLdTma || W <= 256, "TMA boxes are at most 256 elements wide");
     static_assert(!SI::is2d || (TYT == 1 && VY == 1), "rank-2 tiles are one row");
 };
@@ -392,6 +403,11 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
     const int own = (ty * VY + RY) * W + cx;
     constexpr bool SEP = C::SI::sep;
     TC q[VY][(STAR || SEP) ? 2 * R + 1 : 1];  // z-queue, q[v][R + dz]: star: raw values; sep: xy-filtered
+    // Float-pair 3D sweeps (standalone launches): a thread's points are
+    // summed two rows at a time (2p, 2p+1) into packed accumulators, acc[p]
+    // of df2 (df2_fma_s in df32.cuh).
+    constexpr bool PACK = C::PACKED && !std::is_same_v<Args, BatchArgs>;
+    constexpr int NPR = PACK ? VY / 2 : 1;
     unsigned range_err = 0;
     const bool x_ok = x0 + tx < a.ub2;
     // output pointer of (zs, y0 + ty*VY, x0 + tx); rows beyond ub1 are masked
@@ -459,7 +475,49 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
         }
         const int slot_j = C::CONVERT ? s_cmp : s_stg;
         const TC *cur = cmp_base + slot_j * CMP_STRIDE;
-        if constexpr (SEP) {
+        if constexpr (SEP && PACK) {
+            // as below, rows and points in pairs
+            constexpr int D = 2 * R + 1;
+            constexpr int CX0 = 2 * D;
+            constexpr int NROW = VY + 2 * R;
+            TC xr[NROW];
+#pragma unroll
+            for (int i = 0; i < NROW; i += 2) {
+                const TC *r0 = cur + own + (i - R) * W, *r1 = r0 + W;
+                df2 t;
+                float2 c = coef_f2<C>(a, CX0);
+                df2_mul_s(t, c.x, c.y, r0[-R], r1[-R]);
+#pragma unroll
+                for (int dx = -R + 1; dx <= R; ++dx) {
+                    c = coef_f2<C>(a, CX0 + dx + R);
+                    df2_fma_s(t, c.x, c.y, r0[dx], r1[dx]);
+                }
+                u64 hh, ll;
+                renorm2(t, hh, ll);
+                upk2(hh, xr[i].x, xr[i + 1].x);
+                upk2(ll, xr[i].y, xr[i + 1].y);
+            }
+#pragma unroll
+            for (int v = 0; v < VY; v += 2) {
+#pragma unroll
+                for (int k = 0; k < 2 * R; ++k) {
+                    q[v][k] = q[v][k + 1];
+                    q[v + 1][k] = q[v + 1][k + 1];
+                }
+                df2 t;
+                float2 c = coef_f2<C>(a, D);
+                df2_mul_s(t, c.x, c.y, xr[v], xr[v + 1]);
+#pragma unroll
+                for (int dy = -R + 1; dy <= R; ++dy) {
+                    c = coef_f2<C>(a, D + dy + R);
+                    df2_fma_s(t, c.x, c.y, xr[v + R + dy], xr[v + 1 + R + dy]);
+                }
+                u64 hh, ll;
+                renorm2(t, hh, ll);
+                upk2(hh, q[v][2 * R].x, q[v + 1][2 * R].x);
+                upk2(ll, q[v][2 * R].y, q[v + 1][2 * R].y);
+            }
+        } else if constexpr (SEP) {
             // xy-filter the arriving plane for this thread's points and push
             // the results into the z-queue: x pass per row (rows of the point
             // column plus the y halo), then y pass (rank 3 only).
@@ -501,7 +559,107 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                 q[v][2 * R] = cur[own + v * W];
             }
         }
-        if (j >= 2 * R) {
+        if constexpr (PACK) {
+            if (j >= 2 * R) {
+                // The scalar sweep below with the sums of rows 2p and 2p+1
+                // packed: per point the same terms in the same order and the
+                // same roundings.
+                df2 acc[NPR];
+                if constexpr (SEP) {
+#pragma unroll
+                    for (int p = 0; p < NPR; ++p) {
+                        float2 c = coef_f2<C>(a, 0);
+                        df2_mul_s(acc[p], c.x, c.y, q[2 * p][0], q[2 * p + 1][0]);
+#pragma unroll
+                        for (int dz = 1; dz < 2 * R + 1; ++dz) {
+                            c = coef_f2<C>(a, dz);
+                            df2_fma_s(acc[p], c.x, c.y, q[2 * p][dz], q[2 * p + 1][dz]);
+                        }
+                    }
+                } else if constexpr (STAR) {
+                    const int sl = slot_j >= R ? slot_j - R : slot_j - R + NRING;
+                    const TC *pl = cmp_base + sl * CMP_STRIDE;
+#pragma unroll
+                    for (int p = 0; p < NPR; ++p) {
+                        const float2 c = coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, 0, 0));
+                        df2_mul_s(acc[p], c.x, c.y, q[2 * p][R], q[2 * p + 1][R]);
+                    }
+#pragma unroll
+                    for (int d = 1; d <= R; ++d)
+#pragma unroll
+                        for (int p = 0; p < NPR; ++p) {
+                            const float2 cm = coef_f2<C>(a, coef_slot<C::SHAPE, R>(-d, 0, 0));
+                            const float2 cp = coef_f2<C>(a, coef_slot<C::SHAPE, R>(d, 0, 0));
+                            df2_fma_s(acc[p], cm.x, cm.y, q[2 * p][R - d], q[2 * p + 1][R - d]);
+                            df2_fma_s(acc[p], cp.x, cp.y, q[2 * p][R + d], q[2 * p + 1][R + d]);
+                        }
+                    TC col[VY + 2 * R];
+#pragma unroll
+                    for (int i = 0; i < VY + 2 * R; ++i) col[i] = pl[own + (i - R) * W];
+#pragma unroll
+                    for (int d = 1; d <= R; ++d)
+#pragma unroll
+                        for (int p = 0; p < NPR; ++p) {
+                            const float2 cm = coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, -d, 0));
+                            const float2 cp = coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, d, 0));
+                            df2_fma_s(acc[p], cm.x, cm.y, col[2 * p + R - d], col[2 * p + 1 + R - d]);
+                            df2_fma_s(acc[p], cp.x, cp.y, col[2 * p + R + d], col[2 * p + 1 + R + d]);
+                        }
+#pragma unroll
+                    for (int d = 1; d <= R; ++d)
+#pragma unroll
+                        for (int p = 0; p < NPR; ++p) {
+                            const TC *r0 = pl + own + 2 * p * W, *r1 = r0 + W;
+                            const float2 cm = coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, 0, -d));
+                            const float2 cp = coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, 0, d));
+                            df2_fma_s(acc[p], cm.x, cm.y, r0[-d], r1[-d]);
+                            df2_fma_s(acc[p], cp.x, cp.y, r0[d], r1[d]);
+                        }
+                } else {
+#pragma unroll
+                    for (int dz = -R; dz <= R; ++dz) {
+                        const int back = R - dz;
+                        const int sl = slot_j >= back ? slot_j - back : slot_j - back + NRING;
+                        const TC *pl = cmp_base + sl * CMP_STRIDE;
+#pragma unroll
+                        for (int dx = -R; dx <= R; ++dx) {
+                            TC col[VY + 2 * R];
+#pragma unroll
+                            for (int i = 0; i < VY + 2 * R; ++i) col[i] = pl[own + (i - R) * W + dx];
+#pragma unroll
+                            for (int dy = -R; dy <= R; ++dy)
+#pragma unroll
+                                for (int p = 0; p < NPR; ++p) {
+                                    const float2 c = coef_f2<C>(a, coef_slot<C::SHAPE, R>(dz, dy, dx));
+                                    if (dz == -R && dx == -R && dy == -R)
+                                        df2_mul_s(acc[p], c.x, c.y, col[2 * p + R + dy], col[2 * p + 1 + R + dy]);
+                                    else
+                                        df2_fma_s(acc[p], c.x, c.y, col[2 * p + R + dy], col[2 * p + 1 + R + dy]);
+                                }
+                        }
+                    }
+                }
+#pragma unroll
+                for (int p = 0; p < NPR; ++p) {
+                    float h0, h1, l0, l1;
+                    if constexpr (C::ST == kStF32x2) {
+                        u64 hh, ll;
+                        renorm2(acc[p], hh, ll);
+                        upk2(hh, h0, h1);
+                        upk2(ll, l0, l1);
+                        if (2 * p < vmax) optr[2 * p * a.out_s1] = make_float2(h0, l0);
+                        if (2 * p + 1 < vmax) optr[(2 * p + 1) * a.out_s1] = make_float2(h1, l1);
+                    } else {
+                        upk2(acc[p].h, h0, h1);
+                        upk2(acc[p].l, l0, l1);
+                        if (2 * p < vmax) A::store(optr + 2 * p * a.out_s1, df{h0, l0}, range_err, pair_bias(a.pair_shift));
+                        if (2 * p + 1 < vmax)
+                            A::store(optr + (2 * p + 1) * a.out_s1, df{h1, l1}, range_err, pair_bias(a.pair_shift));
+                    }
+                }
+                optr += a.out_s0;
+            }
+        } else if (j >= 2 * R) {
             Acc acc[VY];
             if constexpr (SEP) {
 #pragma unroll

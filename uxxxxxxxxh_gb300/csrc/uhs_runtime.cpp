@@ -449,9 +449,14 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
         // have one fixed tile).  GStencil/s new vs old default, z-chunk caps
         // (below) included.
         if (arith == UHS_ARITH_DF32) {
-            if (shape == kStar3) tile = R >= 2 ? 1 : 2;  // 3d2r 118.4 vs 114.7
-            else if (sep) tile = R == 2 ? 1 : 0;         // 3d1r/2r/3r 147/97/64 vs 137/77/52 at 64 x 8
-            else tile = 1;                               // 3d1r box 81.6 vs 75.9
+            // with packed sums (stream_kernel.cuh PACKED), GStencil/s per
+            // sweep at 512^3: float-pair grids of a 3d1r star 341 at 32 x 16
+            // (4 per thread) vs 311 at 64 x 8 (FP64 grids swept in place:
+            // 189 vs 191); 3d2r/3d3r stars 186/134 vs 181/127 at 64 x 8;
+            // separable boxes r1/r2/r3 235/125/79 (FP64 in place 163/102/68)
+            // vs 231/122/76 (162/98/60) at 32 x 32
+            if (shape == kStar3) tile = (R >= 2 || sp.dtype == UHS_F32X2) ? 1 : 2;
+            else tile = 1;  // separable and term-by-term boxes (3d1r box 81.6 vs 75.9 at 32 x 32)
         } else if (sp.dtype == UHS_F32) {
             // 3d1r/2r/3r 632/659/438 vs 596/625/410; 32-row tiles for r2 only
             // when they do not leave more than 2 % of the rows idle (a
