@@ -205,6 +205,18 @@ int uhs_sweep(const uhs_stencil_desc *desc, const uhs_memref *in, const uhs_memr
 int uhs_plan(const uhs_stencil_desc *desc, const uhs_memref *a, const uhs_params *params,
              uhs_params *out);
 
+/* Geometry of the streaming launch uhs_plan describes, for cost models:
+ *   out[0] = z-chunk (planes, or rows of a rank-2 grid, per CTA)
+ *   out[1] = resident CTAs per SM of the kernel variant
+ *   out[2] = CTAs in the launch            out[3] = SMs of the current device
+ * out[0..2] are 0 when the plan is not a streaming launch.  Occupancy comes
+ * from the CUDA runtime's query (1 where it cannot answer, e.g. without a
+ * GPU).  The z-chunk the reference fixes at compile time through its
+ * tile_sizes_l0 (include/Conversion/UHAffineToParallel/Passes.td:6-101) is
+ * chosen here at run time. */
+int uhs_launch_geometry(const uhs_stencil_desc *desc, const uhs_memref *a, const uhs_params *params,
+                        int64_t out[4]);
+
 /* FP64 error of grid x against the FP64 grid ref over desc's domain, reduced
  * on the GPU (the comparison the reference's drivers do on the host after a
  * run, UH-GPU/3d1r_star/3d7pt_main.cpp:84-96, here for x of any element type):

@@ -5,8 +5,10 @@ programs drawn from another seed, which it never saw; each program is also
 tuned exhaustively (the yardstick).  Compared with the methods without it:
 
 * an uninformed pick (the median candidate): the network's pick is faster;
-* exhaustive tuning: the network's three best-ranked candidates, timed
-  (3 timings instead of dozens), keep almost all of the exhaustive best.
+* exhaustive tuning: on each of the 12 shapes the learned tuner's pick --
+  the network's three best-ranked candidates, timed (3 timings instead of
+  dozens) -- reaches at least 95 % of the exhaustive best on every program;
+  the network's pick alone (no timing) at least 90 %, 97 % on average.
 
 Set UHS_COSTMODEL_OUT to write the per-program table."""
 import json
@@ -31,14 +33,22 @@ def test_trained_model_gain_on_unseen_programs(cuda):
         a, b = device_grids(st)
         _, results = Tuner().tune(st, a, b, reps=3, push=False)
         ns = sorted(r[0] for r in results)
+        best_p = min(results, key=lambda r: r[0])[1]
         pick = cm.pick(st)
         pick3 = cm.pick_verified(st, a, b, k=3)
         dflt = plan(st, memref_raw(1 << 20, st.sizes), params=RunParams(flags=_lib.UHS_FLAG_NO_TUNE_DB))
         dflt.flags = _lib.UHS_FLAG_NO_TUNE_DB
-        t = {k: min(measure(st, a, b, p, reps=3, min_ms=4.0) for _ in range(2))
-             for k, p in (("mlp", pick), ("mlp_top3", pick3), ("default", dflt))}
-        best = min([ns[0]] + list(t.values()))
-        rows.append({"program": st.name, "dtype": st.dtype, "candidates": len(ns),
+        # the exhaustive winner re-timed with the picks, interleaved, over
+        # >= 4 ms each (the table's own minimum is biased low by its noise)
+        named = (("exhaustive", best_p), ("mlp", pick), ("mlp_top3", pick3), ("default", dflt))
+        acc = {k: [] for k, _ in named}
+        for _ in range(3):
+            for k, p in named:
+                acc[k].append(measure(st, a, b, p, reps=3, min_ms=4.0))
+        t = {k: min(v) for k, v in acc.items()}
+        best = min(t.values())
+        rows.append({"program": st.name, "shape": st.name.split("_", 1)[1], "dtype": st.dtype,
+                     "candidates": len(ns),
                      "best_ns": best, "median_ns": ns[len(ns) // 2], **{k + "_ns": v for k, v in t.items()}})
         del a, b
     if os.environ.get("UHS_COSTMODEL_OUT"):
@@ -49,6 +59,17 @@ def test_trained_model_gain_on_unseen_programs(cuda):
     assert beats_median >= len(rows) - 1, rows
     gain_vs_median = statistics.mean(r["median_ns"] / r["mlp_ns"] for r in rows)
     assert gain_vs_median > 1.2
+    # per shape (12 shapes, an FP64 and an FP32 program each): the learned
+    # tuner's verified pick (the network's three best candidates, timed)
+    # within 5 % of the exhaustive best on every program; the network's
+    # untimed pick within 10 %, and within 3 % on average
+    worst, worst3 = {}, {}
+    for r in rows:
+        worst[r["shape"]] = min(worst.get(r["shape"], 1.0), r["best_ns"] / r["mlp_ns"])
+        worst3[r["shape"]] = min(worst3.get(r["shape"], 1.0), r["best_ns"] / r["mlp_top3_ns"])
+    assert len(worst3) == 12 and min(worst3.values()) >= 0.95, worst3
+    assert min(worst.values()) >= 0.90, worst
+    assert statistics.mean(r["best_ns"] / r["mlp_ns"] for r in rows) >= 0.97, rows
     # top-3 verified picks keep >= 95% of the exhaustive best on average
     assert statistics.mean(r["best_ns"] / r["mlp_top3_ns"] for r in rows) >= 0.95
     # and never fall far behind the planner's own default

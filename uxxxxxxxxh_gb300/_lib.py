@@ -68,6 +68,7 @@ SIGNATURES = {
     "uhs_sweep": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Memref), POINTER(Params), c_void_p]),
     "uhs_plan": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Params), POINTER(Params)]),
     "uhs_launch_count": (c_int64, []),
+    "uhs_launch_geometry": (c_int, [POINTER(StencilDesc), POINTER(Memref), POINTER(Params), POINTER(c_int64)]),
     "uhs_release_scratch": (c_int, []),
     "uhs_probe_wait_timeout": (c_int, [c_int64, c_void_p]),
     "uhs_probe_dfma_rate": (c_int, [POINTER(c_double), c_void_p]),

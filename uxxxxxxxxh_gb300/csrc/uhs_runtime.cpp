@@ -652,6 +652,63 @@ static bool range_ok(const SweepSpec &sp, const GridView &a, const GridView &b, 
     return true;
 }
 
+// CTAs per SM of a streaming launch's kernel variant (1 when the query fails;
+// its error is cleared so the launch does not report it).
+static int stream_occupancy(const StreamCall &c) {
+    int occ = 0;
+    StreamCall q = c;
+    q.occ_out = &occ;
+    if (stream_dispatch(q) != cudaSuccess || occ <= 0) {
+        cudaGetLastError();
+        occ = 1;
+    }
+    return occ;
+}
+
+// z-chunk of a streaming launch: the caller's tile_z, else enough CTAs for
+// about four waves over the SMs, at most the planner's cap; at least 32 rows
+// for rank-2 strips (2048^2 to 4096^2 FP32 5-point: 340 / 507 GStencil/s at
+// 32 rows against 291 / 454 at the 8 rows four waves would give).  *occ_out,
+// when given, receives the variant's CTAs per SM.
+static int stream_zchunk(const SweepSpec &sp, const Plan &pl, const StreamCall &c, int *occ_out) {
+    int bx, by;
+    stream_tile_xy(c, &bx, &by);
+    const int64_t nz = c.ub[0] - c.lb[0];
+    const int64_t tiles = ((c.ub[2] - c.lb[2] + bx - 1) / bx) * ((c.ub[1] - c.lb[1] + by - 1) / by);
+    int zchunk = pl.cfg.tile_z;
+    int occ = 0;
+    if (occ_out || (zchunk <= 0 && nz > 0 && tiles > 0)) occ = stream_occupancy(c);
+    if (zchunk <= 0 && nz > 0 && tiles > 0) {
+        const int64_t want = static_cast<int64_t>(device_sms()) * occ * 4;
+        const int64_t chunks = std::max<int64_t>(1, (want + tiles - 1) / tiles);
+        const int floor_z = std::max(sp.rank == 2 ? 32 : 8, 4 * c.R);
+        zchunk = static_cast<int>(std::max<int64_t>(floor_z, (nz + chunks - 1) / chunks));
+        if (pl.zcap > 0) zchunk = std::min(zchunk, std::max(pl.zcap, floor_z));
+    }
+    if (occ_out) *occ_out = occ;
+    return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(zchunk > 0 ? zchunk : 1, std::max<int64_t>(nz, 1))));
+}
+
+// The launch-frame description of a streaming sweep (no grids or stream).
+static StreamCall stream_call_of(const SweepSpec &sp, const Plan &pl) {
+    StreamCall c{};
+    c.shape = pl.shape;
+    c.R = pl.R;
+    c.st = pl.st;
+    c.ar = pl.ar;
+    c.ld = pl.ld;
+    c.tile = pl.tile;
+    c.coef = pl.coef.data();
+    const bool is2d = sp.rank == 2;
+    c.lb[0] = is2d ? sp.lb[1] : sp.lb[0];
+    c.ub[0] = is2d ? sp.ub[1] : sp.ub[0];
+    c.lb[1] = is2d ? 0 : sp.lb[1];
+    c.ub[1] = is2d ? 1 : sp.ub[1];
+    c.lb[2] = sp.lb[2];
+    c.ub[2] = sp.ub[2];
+    return c;
+}
+
 static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in, const GridView &out,
                         cudaStream_t st, unsigned *err_word = nullptr) {
     if (pl.kernel == UHS_KERNEL_GENERIC) {
@@ -716,27 +773,7 @@ static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in,
             c.ld = kLdCpAsync;
         }
     }
-    // z-chunk: enough CTAs for about four waves over the SMs, at most the
-    // planner's cap; at least 32 rows for rank-2 strips (2048^2 to 4096^2
-    // FP32 5-point: 340 / 507 GStencil/s at 32 rows against 291 / 454 at the
-    // 8 rows four waves would give)
-    int bx, by;
-    stream_tile_xy(c, &bx, &by);
-    const int64_t nz = c.ub[0] - c.lb[0];
-    const int64_t tiles = ((c.ub[2] - c.lb[2] + bx - 1) / bx) * ((c.ub[1] - c.lb[1] + by - 1) / by);
-    int zchunk = pl.cfg.tile_z;
-    if (zchunk <= 0 && nz > 0 && tiles > 0) {
-        int occ = 0;
-        StreamCall q = c;
-        q.occ_out = &occ;
-        if (stream_dispatch(q) != cudaSuccess || occ <= 0) occ = 1;
-        const int64_t want = static_cast<int64_t>(device_sms()) * occ * 4;
-        const int64_t chunks = std::max<int64_t>(1, (want + tiles - 1) / tiles);
-        const int floor_z = std::max(sp.rank == 2 ? 32 : 8, 4 * c.R);
-        zchunk = static_cast<int>(std::max<int64_t>(floor_z, (nz + chunks - 1) / chunks));
-        if (pl.zcap > 0) zchunk = std::min(zchunk, std::max(pl.zcap, floor_z));
-    }
-    c.zchunk = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(zchunk > 0 ? zchunk : 1, std::max<int64_t>(nz, 1))));
+    c.zchunk = stream_zchunk(sp, pl, c, nullptr);
     // 4-byte grids: copy in 8-byte pairs when every row start of the tile is 8-byte aligned
     if (eb == 4 && c.ld == kLdCpAsync) {
         const bool even = ((c.lb[2] - c.R) % 2 == 0) && c.in.s[0] % 2 == 0 && c.in.s[1] % 2 == 0 &&
@@ -1675,6 +1712,34 @@ int uhs_plan(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_params *p
     }
     out->tile_z = pl.cfg.tile_z;
     out->k_temporal = pl.cfg.k_temporal;
+    return UHS_OK;
+}
+
+int uhs_launch_geometry(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_params *p, int64_t out[4]) {
+    int rc = validate_desc(d);
+    if (rc) return rc;
+    if (!out) return set_error(UHS_EINVAL, "out is NULL");
+    uhs_params tuned;
+    p = effective_params(d, p, &tuned);
+    SweepSpec sp;
+    make_spec(d, &sp);
+    GridView v{};
+    if (a && (rc = view_of(d, a, "a", &v))) return rc;
+    Plan pl;
+    if ((rc = plan_sweep(sp, p, v, &pl))) return rc;
+    out[0] = out[1] = out[2] = 0;
+    out[3] = device_sms();
+    if (pl.kernel != UHS_KERNEL_STREAM) return UHS_OK;
+    StreamCall c = stream_call_of(sp, pl);
+    int occ = 1;
+    const int zc = stream_zchunk(sp, pl, c, &occ);
+    int bx, by;
+    stream_tile_xy(c, &bx, &by);
+    const int64_t tiles = ((c.ub[2] - c.lb[2] + bx - 1) / bx) * ((c.ub[1] - c.lb[1] + by - 1) / by);
+    const int64_t nz = c.ub[0] - c.lb[0];
+    out[0] = zc;
+    out[1] = occ;
+    out[2] = tiles * ((nz + zc - 1) / zc);
     return UHS_OK;
 }
 

@@ -110,6 +110,18 @@ def plan(stencil: Stencil, a=None, params: RunParams | None = None) -> RunParams
     return RunParams.from_c(out)
 
 
+def launch_geometry(stencil: Stencil, a=None, params: RunParams | None = None) -> dict:
+    """The planned streaming launch's z-chunk, CTAs per SM, CTA count and the
+    device's SM count (uhs_launch_geometry)."""
+    d = stencil.to_desc()
+    out = (ctypes.c_int64 * 4)()
+    p = (params or RunParams()).to_c()
+    ma = (a if isinstance(a, _lib.Memref) else memref_of(a)) if a is not None else None
+    _lib.check(_lib.lib().uhs_launch_geometry(d.ref(), ctypes.byref(ma) if ma is not None else None,
+                                              ctypes.byref(p), out))
+    return {"zchunk": out[0], "ctas_per_sm": out[1], "ctas": out[2], "sms": out[3]}
+
+
 def validate(stencil: Stencil, a, b) -> None:
     d = stencil.to_desc()
     ma = a if isinstance(a, _lib.Memref) else memref_of(a)

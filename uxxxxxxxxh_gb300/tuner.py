@@ -28,7 +28,7 @@ import os
 from dataclasses import asdict
 
 from . import _lib
-from .runtime import RunParams, memref_of, memref_raw, plan
+from .runtime import RunParams, launch_geometry, memref_of, memref_raw, plan
 from .stencil import Stencil
 
 STREAM, GENERIC, MMA = _lib.UHS_KERNEL_STREAM, _lib.UHS_KERNEL_GENERIC, _lib.UHS_KERNEL_MMA
@@ -53,10 +53,33 @@ def class_features(st: Stencil) -> list:
             math.log2(len(st.terms)) / 9.0, float(factored)]
 
 
+def wave_features(st: Stencil, p: RunParams) -> list:
+    """How a streaming launch fills the GPU (uhs_launch_geometry): log2 of its
+    waves (CTAs over SMs x resident CTAs per SM), the occupied fraction of the
+    last wave, and the filled fraction of the last z-chunk.  On small and
+    irregular grids these decide between z-chunks of similar cost."""
+    if p.kernel != STREAM:
+        return [0.0, 0.0, 0.0]
+    try:
+        g = launch_geometry(st, memref_raw(1 << 20, st.sizes), p)
+    except _lib.UhsError:
+        return [0.0, 0.0, 0.0]
+    if g["ctas"] <= 0:
+        return [0.0, 0.0, 0.0]
+    slots = max(1, g["sms"] * g["ctas_per_sm"])
+    waves = g["ctas"] / slots
+    tail = waves - math.floor(waves)
+    nz = max(1, st.ub[0] - st.lb[0]) if st.rank == 3 else max(1, st.ub[1] - st.lb[1])
+    zc = max(1, g["zchunk"])
+    last = (nz % zc) / zc if nz % zc else 1.0
+    return [math.log2(max(waves, 1.0 / 64)) / 6.0, tail if tail > 0 else 1.0, last]
+
+
 def config_features(p: RunParams, st: Stencil | None = None) -> list:
     """Launch features of a planned configuration: tile one-hot, loader,
     arithmetic, z-chunk, generic kernel, and (given the program) how the tile
-    quantises its domain: log2 CTA tiles and the idle fraction of edge tiles."""
+    quantises its domain: log2 CTA tiles and the idle fraction of edge tiles,
+    and how the launch's CTAs fill the GPU (wave_features)."""
     tile = [0.0] * (len(TILES3) + len(TILES2))
     if p.kernel == STREAM:
         if p.tile_y > 1:
@@ -72,12 +95,13 @@ def config_features(p: RunParams, st: Stencil | None = None) -> list:
         tx_n, ty_n = math.ceil(ext[2] / p.tile_x), math.ceil(ext[1] / ty) if st.rank == 3 else 1
         quant = [math.log2(tx_n * ty_n) / 16.0, tx_n * p.tile_x / ext[2] - 1.0,
                  (ty_n * ty / ext[1] - 1.0) if st.rank == 3 else 0.0]
+    waves = wave_features(st, p) if st is not None else [0.0, 0.0, 0.0]
     return tile + [1.0 if p.use_tma == 1 else 0.0, 1.0 if p.arith == _lib.UHS_ARITH_DF32 else 0.0,
                    math.log2(p.tile_z) / 10.0 if p.tile_z > 0 else 0.0, 1.0 if p.kernel == GENERIC else 0.0,
-                   1.0 if p.kernel == MMA else 0.0] + quant
+                   1.0 if p.kernel == MMA else 0.0] + quant + waves
 
 
-N_FEATURES = 9 + 16
+N_FEATURES = 9 + 19
 
 
 def features(st: Stencil, p: RunParams, cls: list | None = None) -> list:

@@ -1,12 +1,13 @@
 """Train the learned cost model on the tuner's own GB300 timings and measure its
 picks against exhaustive tuning.
 
-    python -m uxxxxxxxxh_gb300.tuner_study [--train N] [--test M] [--out result.json]
+    python -m uxxxxxxxxh_gb300.tuner_study [--train N] [--small S] [--test M] [--out result.json]
                                            [--model costmodel.json]
 
 1. N training programs drawn from a seed across the 12 shapes and FP32/FP64,
    extents log-uniform (3D sides 48-384, 2D sides 512-6144, each axis drawn
-   separately), each tuned exhaustively: every timing becomes a record.
+   separately), and S more on small, irregular grids (3D sides 24-128, 2D
+   256-2048), each tuned exhaustively: every timing becomes a record.
 2. The network (costmodel.CostModel, the library's MLP kernels) is trained
    on the GPU on those records.
 3. M held-out programs from another seed, at least one per shape and element
@@ -37,7 +38,11 @@ from .workloads import normalised, splitmix_uniform
 SHAPES12 = [(rank, r, kind) for rank in (2, 3) for kind in ("star", "box") for r in (1, 2, 3)]
 
 
-def draw_programs(n: int, seed: int, cover: bool = False) -> list:
+def draw_programs(n: int, seed: int, cover: bool = False, small: bool = False) -> list:
+    """n programs from the seed: shape and element type drawn (or, with cover,
+    cycling through the 12 shapes in FP64 and FP32), extents log-uniform per
+    axis; `small` draws the small and irregular grids (3D sides 24-128, 2D
+    256-2048) where the launch's wave quantisation decides."""
     u = splitmix_uniform(seed, n * 8)
     out = []
     for g in range(n):
@@ -49,8 +54,10 @@ def draw_programs(n: int, seed: int, cover: bool = False) -> list:
             rank, r, kind = SHAPES12[min(11, int(v[0] * 12))]
             f64 = v[4] >= 0.5
         lo, hi = (512, 6144) if rank == 2 else (48, 384)
+        if small:
+            lo, hi = (256, 2048) if rank == 2 else (24, 128)
         if rank == 3 and kind == "box" and r >= 2:
-            hi = 192  # keep the slow native-FP64 boxes within seconds of timing
+            hi = min(hi, 192)  # keep the slow native-FP64 boxes within seconds of timing
         sides = [int(round(math.exp(math.log(lo) + x * (math.log(hi) - math.log(lo))))) for x in v[1:1 + rank]]
         offs = star_offsets(rank, r) if kind == "star" else box_offsets(rank, r)
         coefs = normalised(splitmix_uniform(seed * 977 + g, len(offs)) + 0.05)
@@ -60,10 +67,10 @@ def draw_programs(n: int, seed: int, cover: bool = False) -> list:
 
 
 def run(n_train: int, n_test: int, reps: int, epochs: int, out: str | None, model_path: str | None,
-        seed: int = 101) -> dict:
+        seed: int = 101, n_small: int = 0) -> dict:
     t0 = time.time()
     tr = Tuner()
-    for st in draw_programs(n_train, seed):
+    for st in draw_programs(n_train, seed) + draw_programs(n_small, seed + 50, small=True):
         a, b = device_grids(st)
         tr.tune(st, a, b, reps=reps, push=False)
         del a, b
@@ -101,7 +108,8 @@ def run(n_train: int, n_test: int, reps: int, epochs: int, out: str | None, mode
         by_shape[k] = min(by_shape.get(k, 1e9), r["mlp_gst"] / r["best_gst"])
         by_shape3[k] = min(by_shape3.get(k, 1e9), r["mlp_top3_gst"] / r["best_gst"])
     gains = [(r["mlp_gst"] or 0.0) / r["default_gst"] for r in rows if r["default_gst"]]
-    res = {"train_programs": n_train, "records": len(tr.records), "final_train_loss": loss,
+    res = {"train_programs": n_train, "small_train_programs": n_small, "records": len(tr.records),
+           "final_train_loss": loss,
            "collect_seconds": t_collect, "train_seconds": t_train, "test_programs": n_test,
            "worst_ratio_by_shape": by_shape, "worst_ratio": min(by_shape.values()),
            "worst_ratio_top3_by_shape": by_shape3, "worst_ratio_top3": min(by_shape3.values()),
@@ -121,13 +129,14 @@ def run(n_train: int, n_test: int, reps: int, epochs: int, out: str | None, mode
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--train", type=int, default=120)
+    ap.add_argument("--small", type=int, default=0, help="extra training programs on small, irregular grids")
     ap.add_argument("--test", type=int, default=24)
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--epochs", type=int, default=300)
     ap.add_argument("--out", default=None)
     ap.add_argument("--model", default=None)
     a = ap.parse_args()
-    res = run(a.train, a.test, a.reps, a.epochs, a.out, a.model)
+    res = run(a.train, a.test, a.reps, a.epochs, a.out, a.model, n_small=a.small)
     print(json.dumps({k: v for k, v in res.items() if k != "rows"}))
 
 
