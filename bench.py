@@ -685,10 +685,13 @@ def main():
             pk_ms = sweep_launch_ms(uhs, st, dev_a, dev_b, pplan, stream, n=10)
             dfma = uhs.probe_dfma_rate(stream)
         gst_p = pts / (msp * 1e-3) / 1e9
+        # DFMA per point of the planned sweep: one per term, or per term of
+        # the 1D passes when a separable box is swept as such
+        dfma_pt = st.rank * (2 * max(st.radius) + 1) if pplan.factored == 1 else len(st.terms)
         plain = {"value": gst_p, "unit": "GStencil/s", "arith": ARITH_LABELS[1], "ms_per_step": msp,
                  "kernel_ms": pk_ms, "hbm_frac": alg_bytes / (pk_ms * 1e-3) / 1e9 / peak,
-                 "dfma_per_s_measured": dfma,
-                 "dfma_frac": st.interior_points * len(st.terms) / (pk_ms * 1e-3) / dfma,
+                 "dfma_per_s_measured": dfma, "dfma_per_point": dfma_pt,
+                 "dfma_frac": st.interior_points * dfma_pt / (pk_ms * 1e-3) / dfma,
                  "bound": "fp64 pipe (one DFMA per term and point)"}
         if errs is not None:
             dev_a.copy_(torch.from_numpy(a0.reshape(st.sizes)))
