@@ -596,10 +596,8 @@ def main():
     # their sweeps are the float-pair kernel on float-pair copies of the
     # grids, so that is the kernel timed here (8-byte pairs: the same 16 B
     # per point-update).
-    star = all(sum(1 for v in t[:3] if v) <= 1 for t in st.terms)
     pair_resident = (st.dtype == uhs.UHS_F64 and plan.kernel == uhs.UHS_KERNEL_STREAM and
-                     plan.arith == uhs._lib.UHS_ARITH_DF32 and st.iterations >= 8 and plan.k_temporal <= 1 and
-                     (plan.factored == 1 or (star and max(st.radius) <= 2)))
+                     plan.arith == uhs._lib.UHS_ARITH_DF32 and st.iterations >= 8 and plan.k_temporal <= 1)
     with torch.cuda.stream(stream):
         if pair_resident:
             hi = dev_a.float()

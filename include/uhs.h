@@ -175,8 +175,8 @@ int uhs_validate(const uhs_stencil_desc *desc, const uhs_memref *a, const uhs_me
  * stream has drained, which is what the reference's entry does.
  *
  * Pair-resident runs: FP64 grids swept in float-pair arithmetic (UHS_ARITH_AUTO
- * after its range check, or UHS_ARITH_DF32) with T >= 8 sweeps of a star of
- * radius 1-2 or a separable box run on float-pair copies of the grids.  Each value is split into its {hi, lo}
+ * after its range check, or UHS_ARITH_DF32) with T >= 8 sweeps on the
+ * streaming kernel (star and box stencils) run on float-pair copies of the grids.  Each value is split into its {hi, lo}
  * floats once, the T sweeps read and write pairs, and the domain of both grids
  * is joined back to FP64 at the end.  The halo is read from the FP64 grids and
  * never written, so it stays bit-exact.  The copies (16 bytes per grid cell)

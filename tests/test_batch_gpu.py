@@ -121,15 +121,16 @@ def test_large_grids_run_as_their_own_launches_beside_the_persistent_kernel(cuda
 def test_large_float_pair_grid_runs_pair_resident_in_the_batch(cuda):
     """A large FP64 7-point star with T = 8 runs pair-resident inside the
     batch (split, 8 sweeps on pairs, join: 12 launches), beside a large FP64
-    19-point star that stays in place; both match the oracle, halos
-    bit-exact, and a second replay continues from the first."""
+    19-point star of T = 6 that stays in place (below 8 sweeps the
+    conversions would not pay); both match the oracle, halos bit-exact, and a
+    second replay continues from the first."""
     small = cfg5_specs(n_grids=4, T=2, seed=19, side2=(40, 100), side3=(12, 24))
     big1, _ = random_case(3, 1, "star", (136, 128, 128), 8, 41)
-    big2, _ = random_case(3, 3, "star", (130, 130, 130), 8, 42)
+    big2, _ = random_case(3, 3, "star", (130, 130, 130), 6, 42)
     specs = small + [(big1, 401), (big2, 402)]
     a, b, host = _grids(specs)
     batch = uhs.Batch([s for s, _ in specs], a, b)
-    assert batch.stats()["launches"] == 2 + (8 + 4) + 8
+    assert batch.stats()["launches"] == 2 + (8 + 4) + 6
     batch.run()
     _check(specs, a, b, host)
     for (st, _), da, db in zip(specs[-2:], a[-2:], b[-2:]):

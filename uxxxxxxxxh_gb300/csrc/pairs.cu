@@ -2,8 +2,8 @@
 // The pairs may hold the values scaled by a power of two (df32.cuh): the
 // split applies the run's scale and the join removes it.
 //
-// A program of T >= 8 float-pair sweeps on FP64 grids (a star of radius 1-2
-// or a separable box; pair_eligible in uhs_runtime.cpp) runs on float-pair
+// A program of T >= 8 float-pair sweeps on FP64 grids (pair_eligible in
+// uhs_runtime.cpp) runs on float-pair
 // copies of its grids: each FP64 value is split once
 // (split_f64) into a {hi, lo} float pair, the T sweeps read and write pairs
 // (no split on every load, no join on every store: the sweep kernel's

@@ -993,17 +993,16 @@ static double batch_item_cost(int bx, int by, int zc, int nterms, int st, int ar
 constexpr int64_t kSoloPoints = int64_t(1) << 21;
 constexpr int kSoloBranches = 4;
 // Float-pair FP64 programs that run pair-resident (uhs_run in uhs.h; the
-// batches' solo grids): T >= kPairMinT sweeps of a star of radius 1-2 or a
-// separable box, where that measured faster on GB300 (3d7pt 180 -> 278,
-// 3d13pt 119 -> 182, 2d5pt 183 -> 269 GStencil/s; cfg3's separable
-// 343-point Gaussian 47.9 -> 51.2).  Radius-3 stars and boxes swept term by
-// term gain too little per sweep to pay for the conversions at T = 10
-// (3d19pt 82.4 in place, 80.8 pair-resident; 3d27pt 79.7 / 75.2; 3d343pt
-// 5.73 / 5.15).
+// batches' solo grids): T >= kPairMinT sweeps on the streaming kernel.  The
+// conversions cost a fixed ~1.8 ms per 512^3 grid pair (two splits, two
+// joins, two range scans), and a float-pair sweep saves the split of every
+// loaded value: GB300 at 512^3, T = 10, in place -> pair-resident, ms:
+// 3d7pt 7.42 -> 5.82, 3d13pt 10.69 -> 9.10, 3d19pt 14.23 -> ~11.9 (sweeps
+// 10.05 + conversions), 3d27pt box 16.15 -> ~15.2.  Below T = 8 the
+// conversions would cost more than they save.
 constexpr int kPairMinT = 8;
 static bool pair_eligible(const Plan &pl, int T, const uhs_params *p) {
     return pl.kernel == UHS_KERNEL_STREAM && pl.st == kStF64 && pl.ar == kArDf32 && T >= kPairMinT &&
-           (pl.factored || ((pl.shape == kStar3 || pl.shape == kStar2) && pl.R <= 2)) &&
            !(p && (p->flags & UHS_FLAG_IN_PLACE));
 }
 
