@@ -62,6 +62,7 @@ def parse_args():
     p.add_argument("--arith", type=int, default=0)
     p.add_argument("--kernel", type=int, default=0)
     p.add_argument("--ktemporal", type=int, default=0, help="temporal fusion depth of the main run (1, 2, 4)")
+    p.add_argument("--flags", type=int, default=0, help="UHS_FLAG_* bits added to the main run's parameters")
     p.add_argument("--no-cpu", action="store_true", help="skip the oracle (profiling runs)")
     p.add_argument("--no-fp32", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -268,12 +269,12 @@ def aggregate_gst(points_per_step: int, steps: int, ms: float, world: int) -> fl
     return world * points_per_step * steps / (ms * 1e-3) / 1e9
 
 
-def sweep_launch_ms(uhs, st, a, b, plan, stream, n: int) -> float:
+def sweep_launch_ms(uhs, st, a, b, plan, stream, n: int, flags: int = 0) -> float:
     """Average duration of the sweep kernel alone: n single-sweep calls with
     the planned launch (alternating direction), CUDA events on the stream the
     kernel is launched on."""
     import torch
-    q = uhs.RunParams(**{**plan.__dict__, "flags": uhs._lib.UHS_FLAG_NO_SYNC | uhs._lib.UHS_FLAG_NO_TUNE_DB})
+    q = uhs.RunParams(**{**plan.__dict__, "flags": uhs._lib.UHS_FLAG_NO_SYNC | uhs._lib.UHS_FLAG_NO_TUNE_DB | flags})
     s1 = st.with_(iterations=1)
     uhs.sweep(s1, a, b, q, stream=stream)
     uhs.sweep(s1, b, a, q, stream=stream)
@@ -566,7 +567,7 @@ def main():
 
     st, a0 = make_workload(args)
     params = uhs.RunParams(kernel=args.kernel, arith=args.arith, k_temporal=args.ktemporal,
-                           flags=uhs._lib.UHS_FLAG_NO_SYNC)
+                           flags=uhs._lib.UHS_FLAG_NO_SYNC | args.flags)
     stream = torch.cuda.Stream()
     tdt = torch.float32 if st.dtype == uhs.UHS_F32 else torch.float64
     dev_a = torch.from_numpy(a0.reshape(st.sizes)).to(tdt).cuda()
@@ -606,11 +607,14 @@ def main():
             pb = pa.clone()
             del hi, lo
             st_k = st.with_(dtype=uhs.UHS_F32X2)
-            plan_k = uhs.plan(st_k, pa, uhs.RunParams(kernel=args.kernel, arith=uhs._lib.UHS_ARITH_DF32))
-            kernel_ms = sweep_launch_ms(uhs, st_k, pa, pb, plan_k, stream, n=max(10, min(2 * st.iterations, 40)))
+            plan_k = uhs.plan(st_k, pa, uhs.RunParams(kernel=args.kernel, arith=uhs._lib.UHS_ARITH_DF32,
+                                                      flags=args.flags))
+            kernel_ms = sweep_launch_ms(uhs, st_k, pa, pb, plan_k, stream, n=max(10, min(2 * st.iterations, 40)),
+                                        flags=args.flags)
             del pa, pb
         else:
-            kernel_ms = sweep_launch_ms(uhs, st, dev_a, dev_b, plan, stream, n=max(10, min(2 * st.iterations, 40)))
+            kernel_ms = sweep_launch_ms(uhs, st, dev_a, dev_b, plan, stream, n=max(10, min(2 * st.iterations, 40)),
+                                        flags=args.flags)
     avg_launch_s = kernel_ms * 1e-3
     achieved = alg_bytes / avg_launch_s / 1e9
     step_sweep_ms = ms / max(1, sweeps)
@@ -628,7 +632,8 @@ def main():
         oracle.iterate_f64(st, ra, rb)
         dev_a.copy_(torch.from_numpy(a0.reshape(st.sizes)))
         dev_b.copy_(dev_a)
-        uhs.run(st, dev_a, dev_b, uhs.RunParams(kernel=args.kernel, arith=args.arith, k_temporal=args.ktemporal))
+        uhs.run(st, dev_a, dev_b, uhs.RunParams(kernel=args.kernel, arith=args.arith, k_temporal=args.ktemporal,
+                                                flags=args.flags))
         got = dev_a.double().cpu().numpy().reshape(-1)
         errs = oracle.error(st, ra, got)
         errs["halo_bit_exact"] = oracle.halo_diff(st, ra, got) == 0

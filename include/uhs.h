@@ -147,8 +147,13 @@ enum {
     UHS_FLAG_NO_FACTOR = 4,  /* sweep a separable box term by term, not as 1D passes */
     UHS_FLAG_MMA_TMEM_A = 8, /* tensor-core path: stage the A operand in tensor memory
                                 (tcgen05.cp) instead of reading it from shared memory */
-    UHS_FLAG_IN_PLACE = 16   /* FP64 grids in float pairs: sweep the FP64 grids themselves,
+    UHS_FLAG_IN_PLACE = 16,  /* FP64 grids in float pairs: sweep the FP64 grids themselves,
                                 not pair-resident copies (no scratch; see uhs_run) */
+    UHS_FLAG_XSHUFFLE = 32   /* rank-2 stars on FP32 grids (256-wide strips, cp.async) or
+                                float-pair grids (128-wide; for FP64 grids, the sweeps of
+                                pair-resident runs): x-neighbours from the adjacent lanes by
+                                warp shuffles instead of shared memory (an evaluated
+                                alternative, kept for comparison) */
 };
 
 /* ---- entry points ------------------------------------------------------ */

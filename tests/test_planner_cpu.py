@@ -109,3 +109,18 @@ def test_prefetch_is_the_built_depth():
         with pytest.raises(_lib.UhsError) as ei:
             plan(st, params=RunParams(**bad, **gen))
         assert ei.value.code == F.UHS_EUNSUPPORTED
+
+
+def test_lane_shuffle_flag_is_for_rank2_stars():
+    """UHS_FLAG_XSHUFFLE plans the 256-wide FP32 strip (128 for float pairs)
+    and is refused for other shapes, element types and strip widths."""
+    st, _ = random_case(2, 2, "star", (300, 700), 2, 11, dtype=F.UHS_F32)
+    assert plan(st, memref_raw(1 << 20, st.sizes), params=RunParams(flags=F.UHS_FLAG_XSHUFFLE | F.UHS_FLAG_NO_TUNE_DB)).tile_x == 256
+    for bad in (random_case(3, 1, "star", (40, 40, 40), 2, 12, dtype=F.UHS_F32)[0],
+                random_case(2, 1, "box", (300, 700), 2, 13, dtype=F.UHS_F32)[0],
+                random_case(2, 1, "star", (300, 700), 2, 14)[0].with_(dtype=F.UHS_F64)):
+        with pytest.raises(F.UhsError):
+            plan(bad, memref_raw(1 << 20, bad.sizes), params=RunParams(arith=F.UHS_ARITH_FMA,
+                                                                        flags=F.UHS_FLAG_XSHUFFLE | F.UHS_FLAG_NO_TUNE_DB))
+    with pytest.raises(F.UhsError):
+        plan(st, memref_raw(1 << 20, st.sizes), params=RunParams(tile_x=64, flags=F.UHS_FLAG_XSHUFFLE | F.UHS_FLAG_NO_TUNE_DB))

@@ -11,6 +11,7 @@ import pytest
 
 import oracle
 import uxxxxxxxxh_gb300 as uhs
+from uxxxxxxxxh_gb300 import _lib
 from gpu_util import assert_f64_close, assert_halo_exact, run_gpu, run_oracle
 from uxxxxxxxxh_gb300.workloads import random_case
 
@@ -203,3 +204,41 @@ def test_f32_pair_loads_and_single_loads_agree(cuda):
         ra, _ = run_oracle(st, a32.astype(np.float64))
         ga, _ = run_gpu(st32, a32, uhs.RunParams(kernel=STREAM, use_tma=-1), dtype=torch.float32)
         assert oracle.error(st, ra, ga)["l2_rel"] <= 1e-6
+
+
+@pytest.mark.parametrize("r", [1, 2, 3])
+@pytest.mark.parametrize("dtype", ["f32", "f32x2"])
+def test_lane_shuffle_rank2_stars(cuda, r, dtype):
+    """UHS_FLAG_XSHUFFLE: x-neighbours of rank-2 stars from the adjacent lanes
+    by warp shuffles (edge lanes from shared memory).  The same terms in the
+    same order as the shared-memory sweep: bit-identical to it, and within
+    the element type's bar of the oracle."""
+    import numpy as np
+    import torch
+    st, a0 = random_case(2, r, "star", (157, 700), 4, 90 + r)
+    if dtype == "f32":
+        st = st.with_(dtype=_lib.UHS_F32)
+        data, tdt = a0.astype(np.float32), torch.float32
+    else:
+        hi = a0.astype(np.float32)
+        lo = (a0 - hi.astype(np.float64)).astype(np.float32)
+        data, tdt = np.stack([hi, lo], -1).reshape(-1).view(np.float64), torch.float64
+        st = st.with_(dtype=_lib.UHS_F32X2)
+    flags = _lib.UHS_FLAG_XSHUFFLE
+    assert uhs.plan(st, None, uhs.RunParams(flags=flags)).tile_x == (256 if dtype == "f32" else 128)
+    outs = []
+    for f in (0, flags):
+        p = uhs.plan(st, None, uhs.RunParams(flags=f | _lib.UHS_FLAG_NO_TUNE_DB))
+        p.flags = f | _lib.UHS_FLAG_NO_TUNE_DB
+        p.tile_x = 256 if dtype == "f32" else 128
+        outs.append(run_gpu(st, data, p, dtype=tdt))
+    for x, y in zip(outs[0], outs[1]):
+        assert np.array_equal(x.view(np.uint32 if dtype == "f32" else np.uint64),
+                              y.view(np.uint32 if dtype == "f32" else np.uint64))
+    ra, _ = run_oracle(st, a0 if dtype == "f32x2" else a0.astype(np.float32).astype(np.float64))
+    got = outs[1][0]
+    if dtype == "f32x2":
+        got = got.view(np.float32).reshape(-1, 2).astype(np.float64).sum(1)
+        assert oracle.error(st, ra, got)["max_rel"] <= 1e-12
+    else:
+        assert oracle.error(st, ra, got.astype(np.float64))["l2_rel"] <= 1e-6

@@ -7,6 +7,7 @@ kernels and the host runtime that replaces UHStencil's generated
 """
 from ._lib import (UHS_ARITH_AUTO, UHS_ARITH_DF32, UHS_ARITH_EXACT, UHS_ARITH_FMA, UHS_F32, UHS_F32X2, UHS_F64,
                    UHS_FLAG_IN_PLACE, UHS_FLAG_MMA_TMEM_A, UHS_FLAG_NO_FACTOR, UHS_FLAG_NO_SYNC, UHS_FLAG_NO_TUNE_DB,
+                   UHS_FLAG_XSHUFFLE,
                    UHS_KERNEL_AUTO, UHS_KERNEL_GENERIC, UHS_KERNEL_MMA, UHS_KERNEL_STREAM, UhsError, lib)
 from .runtime import (Batch, RunParams, error_norms, launch_count, launch_geometry, memref_of, memref_raw, plan,
                       probe_dfma_rate,
@@ -17,6 +18,7 @@ from .stencil import (SHAPES, Stencil, box_offsets, make_stencil, offsets_for, p
 __all__ = [
     "UHS_ARITH_AUTO", "UHS_ARITH_DF32", "UHS_ARITH_EXACT", "UHS_ARITH_FMA", "UHS_F32", "UHS_F32X2", "UHS_F64",
     "UHS_FLAG_IN_PLACE", "UHS_FLAG_MMA_TMEM_A", "UHS_FLAG_NO_FACTOR", "UHS_FLAG_NO_SYNC", "UHS_FLAG_NO_TUNE_DB",
+    "UHS_FLAG_XSHUFFLE",
     "UHS_KERNEL_AUTO", "UHS_KERNEL_GENERIC", "UHS_KERNEL_MMA", "UHS_KERNEL_STREAM", "UhsError", "lib",
     "Batch", "RunParams", "error_norms", "launch_count", "launch_geometry", "memref_of", "memref_raw", "plan",
     "probe_dfma_rate",

@@ -25,6 +25,7 @@ UHS_ARITH_AUTO, UHS_ARITH_FMA, UHS_ARITH_EXACT, UHS_ARITH_DF32 = 0, 1, 2, 3
 UHS_KERNEL_AUTO, UHS_KERNEL_GENERIC, UHS_KERNEL_STREAM, UHS_KERNEL_MMA = 0, 1, 2, 3
 # flags
 UHS_FLAG_NO_SYNC, UHS_FLAG_NO_TUNE_DB, UHS_FLAG_NO_FACTOR, UHS_FLAG_MMA_TMEM_A, UHS_FLAG_IN_PLACE = 1, 2, 4, 8, 16
+UHS_FLAG_XSHUFFLE = 32
 
 UHS_MAX_TERMS = 512
 UHS_NOALLOC_MAX_PARTIALS = 8192

@@ -68,6 +68,7 @@ struct StreamCall {
     int shift;
     int pair_loads;
     int pair_shift;  // FP64 grids in float pairs: power-of-two scale of the pairs (0: none)
+    int xshuffle;    // rank-2 stars: x-neighbours by warp shuffles (UHS_FLAG_XSHUFFLE)
     unsigned *err;
     cudaStream_t stream;
     int *occ_out;  // when set: report CTAs per SM of the variant instead of launching

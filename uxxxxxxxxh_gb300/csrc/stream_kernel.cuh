@@ -73,10 +73,11 @@ __host__ __device__ constexpr int coef_slot(int dz, int dy, int dx) {
     return axis * 2 * R + (ad - 1) * 2 + (d > 0 ? 1 : 0);
 }
 
-template <int SHAPE_, int R_, int ST_, int AR_, int LD_, int BX_, int TYT_, int VY_, int PD_>
+// XS: rank-2 stars take their x-neighbours by warp shuffles (UHS_FLAG_XSHUFFLE).
+template <int SHAPE_, int R_, int ST_, int AR_, int LD_, int BX_, int TYT_, int VY_, int PD_, int XS_ = 0>
 struct StreamCfg {
     static constexpr int SHAPE = SHAPE_, R = R_, ST = ST_, AR = AR_, LD = LD_, BX = BX_, TYT = TYT_, VY = VY_,
-                         PD = PD_;
+                         PD = PD_, XS = XS_;
     using SI = ShapeInfo<SHAPE, R>;
     using TS = std::conditional_t<ST == kStF64, double, std::conditional_t<ST == kStF32, float, float2>>;
     static constexpr bool CONVERT = (ST == kStF64 && AR == kArDf32);
@@ -107,6 +108,7 @@ struct StreamCfg {
                                    !(SHAPE == kBox3 && (R == 2 || (R == 1 && ST == kStF32x2)));
     static_assert(LD != kLdTma || W <= 256, "TMA boxes are at most 256 elements wide");
     static_assert(!SI::is2d || (TYT == 1 && VY == 1), "rank-2 tiles are one row");
+    static_assert(!XS || (SI::is2d && SI::star), "lane shuffles: rank-2 stars");
 };
 
 
@@ -158,6 +160,22 @@ __device__ __forceinline__ void tma_load_3d(void *smem, const CUtensorMap *map, 
         "[%5];\n" ::"r"(s),
         "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(b)
         : "memory");
+}
+
+// Lane shuffles of a value of the compute type (float, double or a float pair).
+template <class T>
+__device__ __forceinline__ T shfl_up_tc(T v, int d) {
+    if constexpr (std::is_same_v<T, float2>)
+        return make_float2(__shfl_up_sync(0xffffffffu, v.x, d), __shfl_up_sync(0xffffffffu, v.y, d));
+    else
+        return __shfl_up_sync(0xffffffffu, v, d);
+}
+template <class T>
+__device__ __forceinline__ T shfl_down_tc(T v, int d) {
+    if constexpr (std::is_same_v<T, float2>)
+        return make_float2(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d));
+    else
+        return __shfl_down_sync(0xffffffffu, v, d);
 }
 
 // ---- arithmetic policies -----------------------------------------------
@@ -696,14 +714,31 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                             A::add(acc[v], a, coef_slot<C::SHAPE, R>(0, d, 0), col[v + R + d]);
                         }
                 }
+                if constexpr (IS2D && C::XS) {
+                    // x-neighbours from the lanes d columns away (the warp's
+                    // lanes hold consecutive columns; their centre values are
+                    // in the z-queue), the warp's edge lanes from shared memory
+                    const int lane = tid & 31;
+                    const TC cen = q[0][R];
+                    const TC *row = pl + own;
 #pragma unroll
-                for (int d = 1; d <= R; ++d)
-#pragma unroll
-                    for (int v = 0; v < VY; ++v) {
-                        const TC *row = pl + own + v * W;
-                        A::add(acc[v], a, coef_slot<C::SHAPE, R>(0, 0, -d), row[-d]);
-                        A::add(acc[v], a, coef_slot<C::SHAPE, R>(0, 0, d), row[d]);
+                    for (int d = 1; d <= R; ++d) {
+                        TC lft = shfl_up_tc(cen, d), rgt = shfl_down_tc(cen, d);
+                        if (lane < d) lft = row[-d];
+                        if (lane >= 32 - d) rgt = row[d];
+                        A::add(acc[0], a, coef_slot<C::SHAPE, R>(0, 0, -d), lft);
+                        A::add(acc[0], a, coef_slot<C::SHAPE, R>(0, 0, d), rgt);
                     }
+                } else {
+#pragma unroll
+                    for (int d = 1; d <= R; ++d)
+#pragma unroll
+                        for (int v = 0; v < VY; ++v) {
+                            const TC *row = pl + own + v * W;
+                            A::add(acc[v], a, coef_slot<C::SHAPE, R>(0, 0, -d), row[-d]);
+                            A::add(acc[v], a, coef_slot<C::SHAPE, R>(0, 0, d), row[d]);
+                        }
+                }
             } else {
 #pragma unroll
                 for (int dz = -R; dz <= R; ++dz) {

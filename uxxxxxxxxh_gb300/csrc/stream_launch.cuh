@@ -59,6 +59,20 @@ cudaError_t launch_cfg(const StreamCall &c) {
 template <int SHAPE, int R, int ST, int AR, int LD>
 cudaError_t dispatch_tile(const StreamCall &c) {
     constexpr bool is2d = ShapeInfo<SHAPE, R>::is2d;
+    if constexpr (is2d && ShapeInfo<SHAPE, R>::star && (ST == kStF32 || ST == kStF32x2)) {
+        // lane-shuffle variants: the default strips of FP32 (256, cp.async)
+        // and float-pair grids (128)
+        if (c.xshuffle) {
+            if constexpr (ST == kStF32 && LD == kLdCpAsync)
+                return c.tile == 2 ? launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 256, 1, 1, 4, 1>>(c)
+                                   : cudaErrorInvalidValue;
+            else if constexpr (ST == kStF32x2)
+                return c.tile == 0 ? launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 128, 1, 1, 4, 1>>(c)
+                                   : cudaErrorInvalidValue;
+            else
+                return cudaErrorInvalidValue;
+        }
+    }
     if constexpr (is2d) {
         constexpr int PD = 4;
         switch (c.tile) {

@@ -212,6 +212,7 @@ struct Plan {
     int pair_shift = 0;        // FP64 grids in float pairs: the pairs hold x * 2^pair_shift (range_ok)
     bool factored = false;     // separable box run as 1D passes
     bool a_tmem = false;       // tensor-core path: A operand staged in tensor memory
+    bool xshuffle = false;     // rank-2 stars: x-neighbours by warp shuffles
 };
 
 int device_sm_count() {
@@ -478,6 +479,22 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
             tile = 4;
         }
     }
+    // Lane-shuffle variant (UHS_FLAG_XSHUFFLE): rank-2 stars, built for the
+    // default strips of FP32 grids (256 wide) and float-pair grids (128)
+    pl->xshuffle = false;
+    // (FP64 grids in float pairs: the flag applies to the sweeps of their
+    // pair-resident runs, on float-pair grids)
+    const bool xs_pairs_later = sp.dtype == UHS_F64 && arith == UHS_ARITH_DF32 && is2d && shape == kStar2;
+    if ((p->flags & UHS_FLAG_XSHUFFLE) && !xs_pairs_later) {
+        const bool f32 = sp.dtype == UHS_F32 && arith == UHS_ARITH_FMA, f32x2 = sp.dtype == UHS_F32X2;
+        if (!(is2d && shape == kStar2 && (f32 || f32x2)))
+            return set_error(UHS_EUNSUPPORTED, "lane shuffles cover rank-2 stars on FP32 or float-pair grids");
+        const int want = f32 ? 2 : 0;
+        if (cfg.tile_x != 0 && tile != want)
+            return set_error(UHS_EUNSUPPORTED, "lane shuffles run %d-wide strips on this element type", f32 ? 256 : 128);
+        tile = want;
+        pl->xshuffle = true;
+    }
     pl->tile = tile;
     // Load-ahead depth: built into each variant (2D strips 4 rows; 3D 3
     // planes, 2 for radius 2-3 boxes swept term by term; temporal fusion 2).
@@ -692,6 +709,7 @@ static int stream_zchunk(const SweepSpec &sp, const Plan &pl, const StreamCall &
 // The launch-frame description of a streaming sweep (no grids or stream).
 static StreamCall stream_call_of(const SweepSpec &sp, const Plan &pl) {
     StreamCall c{};
+    c.xshuffle = pl.xshuffle ? 1 : 0;
     c.shape = pl.shape;
     c.R = pl.R;
     c.st = pl.st;
@@ -759,6 +777,7 @@ static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in,
     cudaGetDevice(&dev);
     c.err = err_word ? err_word : stream_error_word(dev, st);
     c.pair_shift = pl.pair_shift;
+    c.xshuffle = pl.xshuffle ? 1 : 0;
     if (!c.err) return set_error(UHS_ENOMEM, "device error word allocation failed");
     const int eb = sp.dtype == UHS_F32 ? 4 : 8;
     CUtensorMap tmap;
