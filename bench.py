@@ -63,6 +63,8 @@ def parse_args():
     p.add_argument("--kernel", type=int, default=0)
     p.add_argument("--ktemporal", type=int, default=0, help="temporal fusion depth of the main run (1, 2, 4)")
     p.add_argument("--flags", type=int, default=0, help="UHS_FLAG_* bits added to the main run's parameters")
+    p.add_argument("--tile-x", type=int, default=0, help="CTA tile along x of the main run (0: planner)")
+    p.add_argument("--vx", type=int, default=0, help="points per thread along x of the main run (rank-2 stars: 2)")
     p.add_argument("--no-cpu", action="store_true", help="skip the oracle (profiling runs)")
     p.add_argument("--no-fp32", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -567,7 +569,7 @@ def main():
 
     st, a0 = make_workload(args)
     params = uhs.RunParams(kernel=args.kernel, arith=args.arith, k_temporal=args.ktemporal,
-                           flags=uhs._lib.UHS_FLAG_NO_SYNC | args.flags)
+                           flags=uhs._lib.UHS_FLAG_NO_SYNC | args.flags, tile_x=args.tile_x, vx=args.vx)
     stream = torch.cuda.Stream()
     tdt = torch.float32 if st.dtype == uhs.UHS_F32 else torch.float64
     dev_a = torch.from_numpy(a0.reshape(st.sizes)).to(tdt).cuda()
@@ -608,7 +610,7 @@ def main():
             del hi, lo
             st_k = st.with_(dtype=uhs.UHS_F32X2)
             plan_k = uhs.plan(st_k, pa, uhs.RunParams(kernel=args.kernel, arith=uhs._lib.UHS_ARITH_DF32,
-                                                      flags=args.flags))
+                                                      flags=args.flags, tile_x=args.tile_x, vx=args.vx))
             kernel_ms = sweep_launch_ms(uhs, st_k, pa, pb, plan_k, stream, n=max(10, min(2 * st.iterations, 40)),
                                         flags=args.flags)
             del pa, pb
@@ -633,7 +635,7 @@ def main():
         dev_a.copy_(torch.from_numpy(a0.reshape(st.sizes)))
         dev_b.copy_(dev_a)
         uhs.run(st, dev_a, dev_b, uhs.RunParams(kernel=args.kernel, arith=args.arith, k_temporal=args.ktemporal,
-                                                flags=args.flags))
+                                                flags=args.flags, tile_x=args.tile_x, vx=args.vx))
         got = dev_a.double().cpu().numpy().reshape(-1)
         errs = oracle.error(st, ra, got)
         errs["halo_bit_exact"] = oracle.halo_diff(st, ra, got) == 0
@@ -789,7 +791,8 @@ def main():
                    "parallelism": "replicas" if world > 1 else "1 GPU", "l2": "inputs larger than L2 (no flush)",
                    "kernel": plan.kernel, "arith": arith_names.get(plan.arith, plan.arith),
                    "tile": ([plan_k.tile_x, plan_k.tile_y, plan_k.tile_z, plan_k.vy] if pair_resident else
-                            [plan.tile_x, plan.tile_y, plan.tile_z, plan.vy]), "k_temporal": plan.k_temporal,
+                            [plan.tile_x, plan.tile_y, plan.tile_z, plan.vy]),
+                   "vx": plan_k.vx if pair_resident else plan.vx, "k_temporal": plan.k_temporal,
                    "pair_resident": pair_resident},
         "pct_hbm_roofline": achieved / peak,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -138,7 +138,9 @@ typedef struct uhs_params {
                              by term and for temporal fusion, 4 rows in 2D; generic: 1).
                              0 or the built depth; uhs_plan reports it */
     int32_t factored;     /* set by uhs_plan: 1 when a separable box runs as 1D passes */
-    int32_t reserved;
+    int32_t vx;           /* points per thread along x: 0 or 1, or 2 for rank-2 stars on FP32
+                             grids or in float pairs (tile_x 128 or 256, the CTA's columns;
+                             256 loads by cp.async) */
 } uhs_params;
 
 enum {

@@ -124,3 +124,45 @@ def test_lane_shuffle_flag_is_for_rank2_stars():
                                                                         flags=F.UHS_FLAG_XSHUFFLE | F.UHS_FLAG_NO_TUNE_DB))
     with pytest.raises(F.UhsError):
         plan(st, memref_raw(1 << 20, st.sizes), params=RunParams(tile_x=64, flags=F.UHS_FLAG_XSHUFFLE | F.UHS_FLAG_NO_TUNE_DB))
+
+
+def test_two_points_along_x_is_for_rank2_stars():
+    """vx = 2 plans the 256-column tile (128 threads, cp.async) by default and
+    the 128-column one on request, for rank-2 stars on FP32 grids or in float
+    pairs; it is refused for rank-3 grids, boxes, native FP64, other widths,
+    and with lane shuffles."""
+    st, _ = random_case(2, 2, "star", (300, 700), 2, 11, dtype=F.UHS_F32)
+    raw = memref_raw(1 << 20, st.sizes)
+    p = plan(st, raw, params=RunParams(vx=2, flags=F.UHS_FLAG_NO_TUNE_DB))
+    assert (p.vx, p.tile_x, p.use_tma) == (2, 256, -1)
+    p = plan(st, raw, params=RunParams(vx=2, tile_x=128, flags=F.UHS_FLAG_NO_TUNE_DB))
+    assert (p.vx, p.tile_x) == (2, 128)
+    pairs = st.with_(dtype=F.UHS_F32X2)
+    assert plan(pairs, raw, params=RunParams(vx=2, flags=F.UHS_FLAG_NO_TUNE_DB)).vx == 2
+    # defaults: float pairs take two points (128 columns by TMA, 256 by
+    # cp.async where TMA cannot load the rows); FP32 only radius 2 by TMA
+    p = plan(pairs, raw, params=NO_DB)
+    assert (p.vx, p.tile_x, p.use_tma) == (2, 128, 1)
+    odd = random_case(2, 2, "star", (300, 701), 2, 11, dtype=F.UHS_F32X2)[0]
+    p = plan(odd, memref_raw(1 << 20, odd.sizes), params=RunParams(use_tma=-1, flags=F.UHS_FLAG_NO_TUNE_DB))
+    assert (p.vx, p.tile_x, p.use_tma) == (2, 256, -1)
+    p = plan(st, raw, params=NO_DB)
+    assert (p.vx, p.tile_x, p.use_tma) == (2, 128, 1)
+    for r in (1, 3):
+        s = random_case(2, r, "star", (300, 700), 2, 11, dtype=F.UHS_F32)[0]
+        assert plan(s, memref_raw(1 << 20, s.sizes), params=NO_DB).vx == 1
+    f64 = st.with_(dtype=F.UHS_F64)
+    assert plan(f64, raw, params=RunParams(vx=2, arith=F.UHS_ARITH_DF32, flags=F.UHS_FLAG_NO_TUNE_DB)).vx == 2
+    bad_cases = [
+        (random_case(3, 1, "star", (40, 40, 40), 2, 12, dtype=F.UHS_F32)[0], {}),
+        (random_case(2, 1, "box", (300, 700), 2, 13, dtype=F.UHS_F32)[0], {}),
+        (f64, dict(arith=F.UHS_ARITH_FMA)),
+        (st, dict(tile_x=64)),
+        (st, dict(flags=F.UHS_FLAG_XSHUFFLE)),
+    ]
+    for bad, kw in bad_cases:
+        kw = {**kw, "flags": kw.get("flags", 0) | F.UHS_FLAG_NO_TUNE_DB}
+        with pytest.raises(F.UhsError):
+            plan(bad, memref_raw(1 << 20, bad.sizes), params=RunParams(vx=2, **kw))
+    with pytest.raises(F.UhsError):
+        plan(st, raw, params=RunParams(vx=3, flags=F.UHS_FLAG_NO_TUNE_DB))

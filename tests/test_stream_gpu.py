@@ -228,9 +228,8 @@ def test_lane_shuffle_rank2_stars(cuda, r, dtype):
     assert uhs.plan(st, None, uhs.RunParams(flags=flags)).tile_x == (256 if dtype == "f32" else 128)
     outs = []
     for f in (0, flags):
-        p = uhs.plan(st, None, uhs.RunParams(flags=f | _lib.UHS_FLAG_NO_TUNE_DB))
-        p.flags = f | _lib.UHS_FLAG_NO_TUNE_DB
-        p.tile_x = 256 if dtype == "f32" else 128
+        p = uhs.RunParams(kernel=STREAM, tile_x=256 if dtype == "f32" else 128, vx=1,
+                          use_tma=-1 if dtype == "f32" else 0, flags=f | _lib.UHS_FLAG_NO_TUNE_DB)
         outs.append(run_gpu(st, data, p, dtype=tdt))
     for x, y in zip(outs[0], outs[1]):
         assert np.array_equal(x.view(np.uint32 if dtype == "f32" else np.uint64),
@@ -242,3 +241,61 @@ def test_lane_shuffle_rank2_stars(cuda, r, dtype):
         assert oracle.error(st, ra, got)["max_rel"] <= 1e-12
     else:
         assert oracle.error(st, ra, got.astype(np.float64))["l2_rel"] <= 1e-6
+
+
+@pytest.mark.parametrize("r", [1, 2, 3])
+@pytest.mark.parametrize("dtype", ["f32", "f32x2", "f64"])
+@pytest.mark.parametrize("tile_x,use_tma", [(128, 0), (128, -1), (256, -1)])
+def test_two_points_along_x_rank2_stars(cuda, r, dtype, tile_x, use_tma):
+    """vx = 2: each thread sweeps two adjacent columns of a rank-2 star
+    (float pairs: the two points' sums packed).  Per point the same terms in
+    the same order and the same roundings as one point per thread: bit-
+    identical to it, on odd widths whose rows alternate between 2-point
+    vector stores and single stores, and within the element type's bar of
+    the oracle."""
+    import torch
+    # odd rows (cp.async): row starts alternate in alignment; even rows let TMA load
+    st, a0 = random_case(2, r, "star", (157, 702 if use_tma == 0 else 701), 4, 120 + r)
+    tdt = torch.float64
+    if dtype == "f32":
+        st = st.with_(dtype=_lib.UHS_F32)
+        data, tdt, arith = a0.astype(np.float32), torch.float32, uhs.UHS_ARITH_FMA
+    elif dtype == "f32x2":
+        hi = a0.astype(np.float32)
+        lo = (a0 - hi.astype(np.float64)).astype(np.float32)
+        data = np.stack([hi, lo], -1).reshape(-1).view(np.float64)
+        st, arith = st.with_(dtype=_lib.UHS_F32X2), uhs.UHS_ARITH_DF32
+    else:
+        data, arith = a0, uhs.UHS_ARITH_DF32
+    base = dict(kernel=STREAM, arith=arith, use_tma=use_tma, flags=_lib.UHS_FLAG_NO_TUNE_DB)
+    one = uhs.RunParams(**base, tile_x=128 if tile_x == 128 else 256 if dtype == "f32" else 128)
+    two = uhs.RunParams(**base, tile_x=tile_x, vx=2)
+    pl = uhs.plan(st, None, two)
+    assert (pl.vx, pl.tile_x) == (2, tile_x)
+    outs = [run_gpu(st, data, p, dtype=tdt) for p in (one, two)]
+    u = np.uint32 if dtype == "f32" else np.uint64
+    for x, y in zip(outs[0], outs[1]):
+        assert np.array_equal(x.view(u), y.view(u))
+    ra, _ = run_oracle(st, a0 if dtype != "f32" else a0.astype(np.float32).astype(np.float64))
+    got = outs[1][0]
+    if dtype == "f32x2":
+        got = got.view(np.float32).reshape(-1, 2).astype(np.float64).sum(1)
+        assert oracle.error(st, ra, got)["max_rel"] <= 1e-12
+    elif dtype == "f64":
+        assert_f64_close(st, ra, got)
+        assert_halo_exact(st, ra, got)
+    else:
+        assert oracle.error(st, ra, got.astype(np.float64))["l2_rel"] <= 1e-6
+
+
+@pytest.mark.parametrize("r", [1, 3])
+def test_two_points_along_x_pair_resident(cuda, r):
+    """vx = 2 carried into the float-pair sweeps of a pair-resident FP64 run
+    (T = 8): bit-identical to one point per thread."""
+    st, a0 = random_case(2, r, "star", (211, 503), 8, 140 + r)
+    outs = [run_gpu(st, a0, uhs.RunParams(kernel=STREAM, flags=_lib.UHS_FLAG_NO_TUNE_DB, **kw))
+            for kw in ({}, {"vx": 2, "tile_x": 256})]
+    for x, y in zip(outs[0], outs[1]):
+        assert np.array_equal(x.view(np.uint64), y.view(np.uint64))
+    ra, _ = run_oracle(st, a0)
+    assert_f64_close(st, ra, outs[1][0])

@@ -56,7 +56,7 @@ class StencilDesc(ctypes.Structure):
 class Params(ctypes.Structure):
     _fields_ = [("kernel", c_int32), ("arith", c_int32), ("tile_x", c_int32), ("tile_y", c_int32),
                 ("tile_z", c_int32), ("k_temporal", c_int32), ("use_tma", c_int32), ("flags", c_int32),
-                ("vy", c_int32), ("prefetch", c_int32), ("factored", c_int32), ("reserved", c_int32)]
+                ("vy", c_int32), ("prefetch", c_int32), ("factored", c_int32), ("vx", c_int32)]
 
 
 # Every symbol include/*.h declares, with its ctypes signature: (restype, argtypes).

@@ -2,7 +2,7 @@
 and the launch's features, so the tuner can rank candidates of a program it
 has never timed.
 
-The network is the library's MLP (include/uhs.h, uhs_mlp_*): 28 features
+The network is the library's MLP (include/uhs.h, uhs_mlp_*): 30 features
 (tuner.features) -> 3 x 64 (ReLU) -> 1, trained on the GPU by the library's own forward, backward
 and Adam kernels on the tuner's timing records (tuner.Tuner.records), five
 of them from different seeds averaged as an ensemble.  Target: log(ns per

@@ -33,6 +33,11 @@ struct StreamArgs {
     int shift;       // TMA box starts this many elements left of x0 - R (16-byte granule)
     int pair_loads;  // cp.async of 4-byte elements in 8-byte pairs (origin and pitches even)
     int pair_shift;  // FP64 grids in float pairs: the pairs hold x * 2^pair_shift (df32.cuh)
+    // two points per thread along x: the tiles start xoff (0 or 1) columns
+    // left of lb2, so each thread's pair of output cells starts on an even
+    // element of the output row (vector stores); cells left of lb2 are not
+    // written
+    int xoff;
     unsigned *err;
     double cd[NT];
     float2 chl[NT];  // float rounding of each coefficient and its rounding error (hi, lo)
@@ -69,6 +74,7 @@ struct StreamCall {
     int pair_loads;
     int pair_shift;  // FP64 grids in float pairs: power-of-two scale of the pairs (0: none)
     int xshuffle;    // rank-2 stars: x-neighbours by warp shuffles (UHS_FLAG_XSHUFFLE)
+    int xoff;        // two points per thread along x: tile origin lb[2] - xoff (StreamArgs::xoff)
     unsigned *err;
     cudaStream_t stream;
     int *occ_out;  // when set: report CTAs per SM of the variant instead of launching
@@ -77,18 +83,27 @@ struct StreamCall {
 // Tile variants: rank-3 (BX, TYT, VY) and rank-2 (BX).
 //   rank 3: 0 = 32 x 32 (VY 4), 1 = 32 x 16 (VY 4), 2 = 64 x 8 (VY 2), 3 = 32 x 16 (VY 2)
 //           (box stencils of radius 2 and 3 always use 32 x 16, VY 2)
-//   rank 2: 0 = 128, 1 = 64, 2 = 256 (cp.async only: a TMA box is <= 256 wide)
+//   rank 2: 0 = 128, 1 = 64, 2 = 256 (cp.async only: a TMA box is <= 256 wide);
+//           stars also 3 = 64 x 2 points along x, 4 = 128 x 2 (cp.async only)
 struct TileShape {
-    int bx, tyt, vy;
+    int bx, tyt, vy, vx;
 };
 inline TileShape tile_shape(bool is2d, int tile) {
-    if (is2d) return tile == 1 ? TileShape{64, 1, 1} : tile == 2 ? TileShape{256, 1, 1} : TileShape{128, 1, 1};
+    if (is2d) {
+        switch (tile) {
+            case 1: return TileShape{64, 1, 1, 1};
+            case 2: return TileShape{256, 1, 1, 1};
+            case 3: return TileShape{64, 1, 1, 2};
+            case 4: return TileShape{128, 1, 1, 2};
+            default: return TileShape{128, 1, 1, 1};
+        }
+    }
     switch (tile) {
-        case 4: return TileShape{32, 4, 8};
-        case 1: return TileShape{32, 4, 4};
-        case 2: return TileShape{64, 4, 2};
-        case 3: return TileShape{32, 8, 2};
-        default: return TileShape{32, 8, 4};
+        case 4: return TileShape{32, 4, 8, 1};
+        case 1: return TileShape{32, 4, 4, 1};
+        case 2: return TileShape{64, 4, 2, 1};
+        case 3: return TileShape{32, 8, 2, 1};
+        default: return TileShape{32, 8, 4, 1};
     }
 }
 
@@ -108,7 +123,7 @@ inline void stream_box(const StreamCall &c, int eb, int *W, int *H) {
     const TileShape t = tile_shape(is2d, c.tile);
     const int q = 16 / eb;
     const bool big_box = (c.shape == kBox3 && c.R >= 2);
-    const int bx = big_box ? 32 : t.bx, by = big_box ? 16 : t.tyt * t.vy;
+    const int bx = big_box ? 32 : t.bx * t.vx, by = big_box ? 16 : t.tyt * t.vy;
     *W = ct_round_up(bx + 2 * c.R + (c.ld == kLdTma ? q - 1 : 0), q);
     *H = by + (is2d ? 0 : 2 * c.R);
 }
@@ -116,7 +131,7 @@ inline void stream_tile_xy(const StreamCall &c, int *bx, int *by) {
     const bool is2d = is_rank2_shape(c.shape);
     const TileShape t = tile_shape(is2d, c.tile);
     const bool big_box = (c.shape == kBox3 && c.R >= 2);
-    *bx = big_box ? 32 : t.bx;
+    *bx = big_box ? 32 : t.bx * t.vx;
     *by = big_box ? 16 : t.tyt * t.vy;
 }
 

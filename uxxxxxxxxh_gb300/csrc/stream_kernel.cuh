@@ -74,10 +74,14 @@ __host__ __device__ constexpr int coef_slot(int dz, int dy, int dx) {
 }
 
 // XS: rank-2 stars take their x-neighbours by warp shuffles (UHS_FLAG_XSHUFFLE).
-template <int SHAPE_, int R_, int ST_, int AR_, int LD_, int BX_, int TYT_, int VY_, int PD_, int XS_ = 0>
+// VX: points per thread along x (rank-2 stars: 1 or 2); a CTA tile is
+// CX = BX * VX columns wide.
+template <int SHAPE_, int R_, int ST_, int AR_, int LD_, int BX_, int TYT_, int VY_, int PD_, int XS_ = 0,
+          int VX_ = 1>
 struct StreamCfg {
     static constexpr int SHAPE = SHAPE_, R = R_, ST = ST_, AR = AR_, LD = LD_, BX = BX_, TYT = TYT_, VY = VY_,
-                         PD = PD_, XS = XS_;
+                         PD = PD_, XS = XS_, VX = VX_;
+    static constexpr int CX = BX * VX;
     using SI = ShapeInfo<SHAPE, R>;
     using TS = std::conditional_t<ST == kStF64, double, std::conditional_t<ST == kStF32, float, float2>>;
     static constexpr bool CONVERT = (ST == kStF64 && AR == kArDf32);
@@ -86,7 +90,7 @@ struct StreamCfg {
     static constexpr int Q = 16 / EB;  // TMA x-coordinate granule, elements
     static constexpr int RY = SI::RY;
     static constexpr int BY = TYT * VY;
-    static constexpr int W = ct_round_up(BX + 2 * R + (LD == kLdTma ? Q - 1 : 0), Q);
+    static constexpr int W = ct_round_up(CX + 2 * R + (LD == kLdTma ? Q - 1 : 0), Q);
     static constexpr int H = BY + 2 * RY;
     static constexpr int NCMP = SI::sep ? 1 : SI::star ? R + 1 : 2 * R + 1;
     static constexpr int NSTG = CONVERT ? PD + 1 : NCMP + PD;
@@ -104,11 +108,15 @@ struct StreamCfg {
     // 7.5/7.2.  Term-by-term boxes of radius 1 on float-pair grids (100 ->
     // 96) and of radius 2 (21.2 -> 20.4, FP64 19.3 -> 19.0) keep the scalar
     // sums.
-    static constexpr bool PACKED = AR == kArDf32 && !SI::is2d && VY % 2 == 0 &&
+    static constexpr bool PACKED = AR == kArDf32 && (SI::is2d ? VX == 2 : VY % 2 == 0) &&
                                    !(SHAPE == kBox3 && (R == 2 || (R == 1 && ST == kStF32x2)));
     static_assert(LD != kLdTma || W <= 256, "TMA boxes are at most 256 elements wide");
     static_assert(!SI::is2d || (TYT == 1 && VY == 1), "rank-2 tiles are one row");
     static_assert(!XS || (SI::is2d && SI::star), "lane shuffles: rank-2 stars");
+    static_assert(VX == 1 || (VX == 2 && SI::is2d && SI::star && !XS), "two points along x: rank-2 stars");
+    // points per thread, and their spacing in shared memory: rows along y
+    // (rank 3), or adjacent columns (rank 2 with VX = 2)
+    static constexpr int NPT = VX == 2 ? 2 : VY;
 };
 
 
@@ -254,6 +262,12 @@ struct Arith<C, kArNative> {
         if constexpr (F32) acc = fmaf(a.cl_sum[pass], v, acc);
     }
     __device__ static __forceinline__ void store(TS *p, const Acc &acc, unsigned &, int) { *p = acc; }
+    // two adjacent points, p aligned to 2 * sizeof(TS)
+    static constexpr bool kVecStore = true;
+    __device__ static __forceinline__ void store2(TS *p, const Acc &a0, const Acc &a1, unsigned &, int) {
+        if constexpr (F32) *reinterpret_cast<float2 *>(p) = make_float2(a0, a1);
+        else *reinterpret_cast<double2 *>(p) = make_double2(a0, a1);
+    }
     __device__ static __forceinline__ TS level(const Acc &acc) { return acc; }
 };
 
@@ -282,6 +296,18 @@ struct Arith<C, kArDf32> {
             *p = renorm(acc);
         }
     }
+    static constexpr bool kVecStore = true;
+    __device__ static __forceinline__ void store2(typename C::TS *p, const Acc &a0, const Acc &a1, unsigned &range_err,
+                                                  int bias) {
+        if constexpr (C::ST == kStF64) {
+            range_err |= (__float_as_uint(a0.h) & 0x7f800000u) == 0x7f800000u;
+            range_err |= (__float_as_uint(a1.h) & 0x7f800000u) == 0x7f800000u;
+            *reinterpret_cast<double2 *>(p) = make_double2(join_f64(a0.h, a0.l, bias), join_f64(a1.h, a1.l, bias));
+        } else {
+            const float2 r0 = renorm(a0), r1 = renorm(a1);
+            *reinterpret_cast<float4 *>(p) = make_float4(r0.x, r0.y, r1.x, r1.y);
+        }
+    }
     __device__ static __forceinline__ float2 level(const Acc &acc) { return renorm(acc); }
     template <class Args>
     __device__ static __forceinline__ void centre(Acc &, const Args &, int, float2) {}
@@ -308,7 +334,8 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
     // another 256-thread block shape (the batched kernel) maps the same way.
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     const int tx = tid % BX, ty = tid / BX;
-    const int64_t x0 = a.lb2 + static_cast<int64_t>(bxi) * BX;
+    constexpr int VX = C::VX, CX = C::CX, NPT = C::NPT;
+    const int64_t x0 = a.lb2 - (VX == 2 ? a.xoff : 0) + static_cast<int64_t>(bxi) * CX;
     const int64_t y0 = a.lb1 + static_cast<int64_t>(byi) * C::BY;
     const int64_t zs = a.lb0 + static_cast<int64_t>(bzi) * a.zchunk;
     const int64_t ze = min(zs + static_cast<int64_t>(a.zchunk), a.ub0);
@@ -335,14 +362,24 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
     int off_a[NLOAD_ROWS], off_b[NLOAD_ROWS];  // 4-byte elements
     unsigned ok_a = 0u, ok_b = 0u;
     const bool pairs = C::EB == 4 && a.pair_loads;  // 8-byte granules, columns 2tx, 2tx+1
-    constexpr int NPAIR = (BX + 2 * R + 1) / 2;
-    const int gxa = static_cast<int>(gx0) + tx, gxb = gxa + BX;
+    constexpr int NPAIR = (CX + 2 * R + 1) / 2;
+    // columns a thread copies: tx, tx + BX and, two points along x, tx + 2BX
+    // (the last one only for the 2R halo columns beyond the tile)
+    const int gxa = static_cast<int>(gx0) + tx, gxb = gxa + BX, gxc = gxb + BX;
     const bool col_a = gxa >= 0 && gxa < a.n2;
-    const bool col_b = tx < 2 * R && gxb < a.n2;
+    const bool col_b = (VX == 2 || tx < 2 * R) && gxb < a.n2;
+    const bool col_c = VX == 2 && tx < 2 * R && gxc < a.n2;
+    int off_c[NLOAD_ROWS];
+    unsigned ok_c = 0u;
+    // pairs mode with two points along x: pair tx and pair tx + BX
+    const bool pair_b = VX == 2 && tx + BX < NPAIR;
     if constexpr (HOIST) {
         const int gx1 = pairs ? static_cast<int>(gx0) + 2 * tx : gxa;
         const bool c1 = pairs ? (tx < NPAIR && gx1 + 1 < a.n2) : col_a;
-        const bool c2 = !pairs && col_b;
+        // second copy: pair tx + BX (pairs mode, two points along x) or column tx + BX
+        const int gx2 = pairs ? gx1 + 2 * BX : gxb;
+        const bool c2 = pairs ? (pair_b && gx2 + 1 < a.n2) : col_b;
+        const bool c3 = !pairs && col_c;
 #pragma unroll
         for (int i = 0; i < NLOAD_ROWS; ++i) {
             const int r = ty + i * TYT;
@@ -350,9 +387,11 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
             const bool row = r < H && gy >= 0 && gy < a.n1;
             const int ro = row ? static_cast<int>(gy * a.in_s1) : 0;
             off_a[i] = row && c1 ? ro + gx1 : 0;
-            off_b[i] = row && c2 ? ro + gxb : 0;
+            off_b[i] = row && c2 ? ro + gx2 : 0;
+            off_c[i] = row && c3 ? ro + gxc : 0;
             ok_a |= static_cast<unsigned>(row && c1) << i;
             ok_b |= static_cast<unsigned>(row && c2) << i;
+            ok_c |= static_cast<unsigned>(row && c3) << i;
         }
     } else {
 #pragma unroll
@@ -376,6 +415,8 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                 for (int i = 0; i < NLOAD_ROWS; ++i) {
                     const int r = ty + i * TYT;
                     if (r < H && tx < NPAIR) cp_async<8>(dst + r * W + 2 * tx, plane + off_a[i], (ok_a >> i) & 1u);
+                    if (VX == 2 && r < H && pair_b)
+                        cp_async<8>(dst + r * W + 2 * (tx + BX), plane + off_b[i], (ok_b >> i) & 1u);
                 }
             } else {
 #pragma unroll
@@ -383,7 +424,10 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                     const int r = ty + i * TYT;
                     if (r < H) {
                         cp_async<C::EB>(dst + r * W + tx, plane + off_a[i], (ok_a >> i) & 1u);
-                        if (tx < 2 * R) cp_async<C::EB>(dst + r * W + tx + BX, plane + off_b[i], (ok_b >> i) & 1u);
+                        if (VX == 2 || tx < 2 * R)
+                            cp_async<C::EB>(dst + r * W + tx + BX, plane + off_b[i], (ok_b >> i) & 1u);
+                        if (VX == 2 && tx < 2 * R)
+                            cp_async<C::EB>(dst + r * W + tx + 2 * BX, plane + off_c[i], (ok_c >> i) & 1u);
                     }
                 }
             }
@@ -396,9 +440,12 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                 if (r < H) {
                     const TS *src = plane + row_off[i];
                     cp_async<C::EB>(dst + r * W + tx, row_ok[i] && col_a ? src + gxa : plane, row_ok[i] && col_a);
-                    if (tx < 2 * R)
+                    if (VX == 2 || tx < 2 * R)
                         cp_async<C::EB>(dst + r * W + tx + BX, row_ok[i] && col_b ? src + gxb : plane,
                                         row_ok[i] && col_b);
+                    if (VX == 2 && tx < 2 * R)
+                        cp_async<C::EB>(dst + r * W + tx + 2 * BX, row_ok[i] && col_c ? src + gxc : plane,
+                                        row_ok[i] && col_c);
                 }
             }
         } else {
@@ -417,21 +464,28 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
         if constexpr (C::LD == kLdCpAsync) cp_commit();
     }
 
-    const int cx = tx + R + a.shift;  // smem column of this thread's x
+    const int cx = VX * tx + R + a.shift;  // smem column of this thread's (first) x
     const int own = (ty * VY + RY) * W + cx;
+    // spacing of a thread's points in shared memory and in the output grid
+    constexpr int PSTEP = VX == 2 ? 1 : W;
+    const int64_t ostep = VX == 2 ? 1 : a.out_s1;
     constexpr bool SEP = C::SI::sep;
-    TC q[VY][(STAR || SEP) ? 2 * R + 1 : 1];  // z-queue, q[v][R + dz]: star: raw values; sep: xy-filtered
+    TC q[NPT][(STAR || SEP) ? 2 * R + 1 : 1];  // z-queue, q[v][R + dz]: star: raw values; sep: xy-filtered
     // Float-pair 3D sweeps (standalone launches): a thread's points are
     // summed two rows at a time (2p, 2p+1) into packed accumulators, acc[p]
     // of df2 (df2_fma_s in df32.cuh).
     constexpr bool PACK = C::PACKED && !std::is_same_v<Args, BatchArgs>;
-    constexpr int NPR = PACK ? VY / 2 : 1;
+    constexpr int NPR = PACK ? NPT / 2 : 1;
     unsigned range_err = 0;
-    const bool x_ok = x0 + tx < a.ub2;
-    // output pointer of (zs, y0 + ty*VY, x0 + tx); rows beyond ub1 are masked
-    TS *optr = static_cast<TS *>(a.out) + zs * a.out_s0 + (y0 + ty * VY) * a.out_s1 + x0 + tx;
-    int vmax = static_cast<int>(min(static_cast<int64_t>(VY), a.ub1 - (y0 + ty * VY)));
+    const bool x_ok = x0 + VX * tx < a.ub2;
+    // output pointer of (zs, y0 + ty*VY, x0 + VX*tx); points vmin..vmax-1
+    // are written: rows beyond ub1 are masked, and with two points along x
+    // columns beyond ub2 and the column left of lb2 (xoff)
+    TS *optr = static_cast<TS *>(a.out) + zs * a.out_s0 + (y0 + ty * VY) * a.out_s1 + x0 + VX * tx;
+    int vmax = VX == 2 ? static_cast<int>(min(static_cast<int64_t>(2), a.ub2 - (x0 + 2 * tx)))
+                       : static_cast<int>(min(static_cast<int64_t>(VY), a.ub1 - (y0 + ty * VY)));
     if (!x_ok) vmax = 0;
+    const int vmin = VX == 2 && x0 + 2 * tx < a.lb2 ? 1 : 0;
 
     int s_stg = 0;       // staging slot of plane j
     unsigned phase = 0;  // mbarrier phase of plane j's slot
@@ -475,8 +529,8 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
         if constexpr (C::LD == kLdCpAsync) cp_commit();
 
         if constexpr (C::CONVERT) {
-            // Columns the loader wrote: the whole TMA box, or BX + 2R for cp.async.
-            constexpr int WL = C::LD == kLdTma ? W : BX + 2 * R;
+            // Columns the loader wrote: the whole TMA box, or CX + 2R for cp.async.
+            constexpr int WL = C::LD == kLdTma ? W : CX + 2 * R;
             const double *sp = reinterpret_cast<const double *>(stg_base + s_stg * STG_ELEMS);
             float2 *dp = cmp_base + s_cmp * CMP_ELEMS;
 #pragma unroll
@@ -571,10 +625,10 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
         }
         if constexpr (STAR) {
 #pragma unroll
-            for (int v = 0; v < VY; ++v) {
+            for (int v = 0; v < NPT; ++v) {
 #pragma unroll
                 for (int k = 0; k < 2 * R; ++k) q[v][k] = q[v][k + 1];
-                q[v][2 * R] = cur[own + v * W];
+                q[v][2 * R] = cur[own + v * PSTEP];
             }
         }
         if constexpr (PACK) {
@@ -611,23 +665,25 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                             df2_fma_s(acc[p], cm.x, cm.y, q[2 * p][R - d], q[2 * p + 1][R - d]);
                             df2_fma_s(acc[p], cp.x, cp.y, q[2 * p][R + d], q[2 * p + 1][R + d]);
                         }
-                    TC col[VY + 2 * R];
+                    if constexpr (!IS2D) {
+                        TC col[VY + 2 * R];
 #pragma unroll
-                    for (int i = 0; i < VY + 2 * R; ++i) col[i] = pl[own + (i - R) * W];
+                        for (int i = 0; i < VY + 2 * R; ++i) col[i] = pl[own + (i - R) * W];
+#pragma unroll
+                        for (int d = 1; d <= R; ++d)
+#pragma unroll
+                            for (int p = 0; p < NPR; ++p) {
+                                const float2 cm = coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, -d, 0));
+                                const float2 cp = coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, d, 0));
+                                df2_fma_s(acc[p], cm.x, cm.y, col[2 * p + R - d], col[2 * p + 1 + R - d]);
+                                df2_fma_s(acc[p], cp.x, cp.y, col[2 * p + R + d], col[2 * p + 1 + R + d]);
+                            }
+                    }
 #pragma unroll
                     for (int d = 1; d <= R; ++d)
 #pragma unroll
                         for (int p = 0; p < NPR; ++p) {
-                            const float2 cm = coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, -d, 0));
-                            const float2 cp = coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, d, 0));
-                            df2_fma_s(acc[p], cm.x, cm.y, col[2 * p + R - d], col[2 * p + 1 + R - d]);
-                            df2_fma_s(acc[p], cp.x, cp.y, col[2 * p + R + d], col[2 * p + 1 + R + d]);
-                        }
-#pragma unroll
-                    for (int d = 1; d <= R; ++d)
-#pragma unroll
-                        for (int p = 0; p < NPR; ++p) {
-                            const TC *r0 = pl + own + 2 * p * W, *r1 = r0 + W;
+                            const TC *r0 = pl + own + 2 * p * PSTEP, *r1 = r0 + PSTEP;
                             const float2 cm = coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, 0, -d));
                             const float2 cp = coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, 0, d));
                             df2_fma_s(acc[p], cm.x, cm.y, r0[-d], r1[-d]);
@@ -665,20 +721,29 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                         renorm2(acc[p], hh, ll);
                         upk2(hh, h0, h1);
                         upk2(ll, l0, l1);
-                        if (2 * p < vmax) optr[2 * p * a.out_s1] = make_float2(h0, l0);
-                        if (2 * p + 1 < vmax) optr[(2 * p + 1) * a.out_s1] = make_float2(h1, l1);
+                        if (VX == 2 && vmin == 0 && vmax == 2 && (reinterpret_cast<uintptr_t>(optr) & 15u) == 0) {
+                            *reinterpret_cast<float4 *>(optr) = make_float4(h0, l0, h1, l1);
+                        } else {
+                            if (2 * p >= vmin && 2 * p < vmax) optr[2 * p * ostep] = make_float2(h0, l0);
+                            if (2 * p + 1 < vmax) optr[(2 * p + 1) * ostep] = make_float2(h1, l1);
+                        }
                     } else {
                         upk2(acc[p].h, h0, h1);
                         upk2(acc[p].l, l0, l1);
-                        if (2 * p < vmax) A::store(optr + 2 * p * a.out_s1, df{h0, l0}, range_err, pair_bias(a.pair_shift));
-                        if (2 * p + 1 < vmax)
-                            A::store(optr + (2 * p + 1) * a.out_s1, df{h1, l1}, range_err, pair_bias(a.pair_shift));
+                        if (VX == 2 && vmin == 0 && vmax == 2 && (reinterpret_cast<uintptr_t>(optr) & 15u) == 0) {
+                            A::store2(optr, df{h0, l0}, df{h1, l1}, range_err, pair_bias(a.pair_shift));
+                        } else {
+                            if (2 * p >= vmin && 2 * p < vmax)
+                                A::store(optr + 2 * p * ostep, df{h0, l0}, range_err, pair_bias(a.pair_shift));
+                            if (2 * p + 1 < vmax)
+                                A::store(optr + (2 * p + 1) * ostep, df{h1, l1}, range_err, pair_bias(a.pair_shift));
+                        }
                     }
                 }
                 optr += a.out_s0;
             }
         } else if (j >= 2 * R) {
-            Acc acc[VY];
+            Acc acc[NPT];
             if constexpr (SEP) {
 #pragma unroll
                 for (int v = 0; v < VY; ++v) {
@@ -691,14 +756,14 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                 const int sl = slot_j >= R ? slot_j - R : slot_j - R + NRING;
                 const TC *pl = cmp_base + sl * CMP_STRIDE;
 #pragma unroll
-                for (int v = 0; v < VY; ++v) {
+                for (int v = 0; v < NPT; ++v) {
                     A::first(acc[v], a, coef_slot<C::SHAPE, R>(0, 0, 0), q[v][R]);
                     A::centre(acc[v], a, 0, q[v][R]);
                 }
 #pragma unroll
                 for (int d = 1; d <= R; ++d)
 #pragma unroll
-                    for (int v = 0; v < VY; ++v) {
+                    for (int v = 0; v < NPT; ++v) {
                         A::add(acc[v], a, coef_slot<C::SHAPE, R>(-d, 0, 0), q[v][R - d]);
                         A::add(acc[v], a, coef_slot<C::SHAPE, R>(d, 0, 0), q[v][R + d]);
                     }
@@ -733,8 +798,8 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
 #pragma unroll
                     for (int d = 1; d <= R; ++d)
 #pragma unroll
-                        for (int v = 0; v < VY; ++v) {
-                            const TC *row = pl + own + v * W;
+                        for (int v = 0; v < NPT; ++v) {
+                            const TC *row = pl + own + v * PSTEP;
                             A::add(acc[v], a, coef_slot<C::SHAPE, R>(0, 0, -d), row[-d]);
                             A::add(acc[v], a, coef_slot<C::SHAPE, R>(0, 0, d), row[d]);
                         }
@@ -773,9 +838,19 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                     }
                 }
             }
+            if constexpr (VX == 2 && A::kVecStore) {
+                // two adjacent columns in one vector store when aligned
+                if (vmin == 0 && vmax == 2 && (reinterpret_cast<uintptr_t>(optr) & (2 * sizeof(TS) - 1)) == 0)
+                    A::store2(optr, acc[0], acc[1], range_err, pair_bias(a.pair_shift));
+                else
 #pragma unroll
-            for (int v = 0; v < VY; ++v)
-                if (v < vmax) A::store(optr + v * a.out_s1, acc[v], range_err, pair_bias(a.pair_shift));
+                    for (int v = 0; v < NPT; ++v)
+                        if (v >= vmin && v < vmax) A::store(optr + v * ostep, acc[v], range_err, pair_bias(a.pair_shift));
+            } else {
+#pragma unroll
+                for (int v = 0; v < NPT; ++v)
+                    if (v >= vmin && v < vmax) A::store(optr + v * ostep, acc[v], range_err, pair_bias(a.pair_shift));
+            }
             optr += a.out_s0;
         }
         // advance the rings

@@ -33,6 +33,7 @@ cudaError_t launch_cfg(const StreamCall &c) {
     a.shift = c.shift;
     a.pair_loads = c.pair_loads;
     a.pair_shift = c.pair_shift;
+    a.xoff = C::VX == 2 ? c.xoff : 0;
     a.err = c.err;
     fill_coefs(a.cd, a.chl, a.cl_sum, c.coef, C::NT, c.shape, c.R);
     const int64_t nz = c.ub[0] - c.lb[0], ny = c.ub[1] - c.lb[1], nx = c.ub[2] - c.lb[2];
@@ -49,7 +50,7 @@ cudaError_t launch_cfg(const StreamCall &c) {
     if (c.occ_out) {
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(c.occ_out, kern, C::THREADS, C::SMEM);
     }
-    dim3 grid(static_cast<unsigned>((nx + C::BX - 1) / C::BX), static_cast<unsigned>((ny + C::BY - 1) / C::BY),
+    dim3 grid(static_cast<unsigned>((nx + a.xoff + C::CX - 1) / C::CX), static_cast<unsigned>((ny + C::BY - 1) / C::BY),
               static_cast<unsigned>((nz + c.zchunk - 1) / c.zchunk));
     kern<<<grid, dim3(C::BX, C::TYT), C::SMEM, c.stream>>>(a);
     count_launch();
@@ -75,7 +76,16 @@ cudaError_t dispatch_tile(const StreamCall &c) {
     }
     if constexpr (is2d) {
         constexpr int PD = 4;
+        // two points along x: stars in float arithmetic (FP32, float pairs)
+        constexpr bool VX2 = ShapeInfo<SHAPE, R>::star && (ST == kStF32 || AR == kArDf32);
         switch (c.tile) {
+            case 3:
+                if constexpr (VX2) return launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 64, 1, 1, PD, 0, 2>>(c);
+                else return cudaErrorInvalidValue;
+            case 4:
+                if constexpr (VX2 && LD == kLdCpAsync)
+                    return launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 128, 1, 1, PD, 0, 2>>(c);
+                else return cudaErrorInvalidValue;
             case 1: return launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 64, 1, 1, PD>>(c);
             case 2:
                 if constexpr (LD == kLdCpAsync) return launch_cfg<StreamCfg<SHAPE, R, ST, AR, LD, 256, 1, 1, PD>>(c);

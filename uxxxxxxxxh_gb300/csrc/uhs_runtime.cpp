@@ -331,6 +331,17 @@ static bool factor_box(const SweepSpec &sp, int R, std::vector<double> *out) {
     return true;
 }
 
+// UHS_ARITH_AUTO after range_ok() vetoed float pairs: native arithmetic.
+// The two-points-along-x tiles of rank-2 stars are built for float
+// arithmetic only; native FP64 takes the 128-column one-point tile.
+static void fall_back_native(Plan &pl) {
+    pl.ar = kArNative;
+    pl.cfg.arith = UHS_ARITH_FMA;
+    if (pl.kernel == UHS_KERNEL_STREAM && pl.st == kStF64 && is_rank2_shape(pl.shape) &&
+        tile_shape(true, pl.tile).vx == 2)
+        pl.tile = 0;
+}
+
 static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &view, Plan *pl) {
     uhs_params dflt;
     uhs_params_default(&dflt);
@@ -431,10 +442,25 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
     // separable boxes run as 1D passes unless the caller opts out
     std::vector<double> fac;
     const bool sep = (shape == kBox3 || shape == kBox2) && !(p->flags & UHS_FLAG_NO_FACTOR) && factor_box(sp, R, &fac);
-    // tile variant from (tile_x, tile_y, vy)
+    // whether the grid allows TMA loads: 16-byte aligned base, row and plane pitches
+    const int eb = sp.dtype == UHS_F32 ? 4 : 8;
+    const int64_t row_b = view.s[1] * eb, plane_b = (is2d ? view.s[1] : view.s[0]) * eb;
+    const bool tma_aligned = !(reinterpret_cast<uintptr_t>(view.data) % 16 || row_b % 16 || plane_b % 16);
+    // tile variant from (tile_x, tile_y, vy, vx)
     int tile = 0;
     pl->zcap = 0;
-    if (is2d) {
+    if (p->vx < 0 || p->vx > 2 || (p->vx == 2 && !is2d))
+        return set_error(UHS_EUNSUPPORTED, "points per thread along x: 1, or 2 for rank-2 stars (got %d)", p->vx);
+    if (is2d && p->vx == 2) {
+        // two points per thread along x: tile 3 (64 threads, 128 columns) or 4 (128 threads, 256)
+        const bool f32 = sp.dtype == UHS_F32 && arith == UHS_ARITH_FMA;
+        if (shape != kStar2 || !(f32 || arith == UHS_ARITH_DF32))
+            return set_error(UHS_EUNSUPPORTED, "two points per thread along x: rank-2 stars on FP32 grids or in "
+                                               "float pairs");
+        if (cfg.tile_x == 128) tile = 3;
+        else if (cfg.tile_x == 0 || cfg.tile_x == 256) tile = 4;
+        else return set_error(UHS_EINVAL, "two points per thread along x: tiles are 128 or 256 wide (got %d)", cfg.tile_x);
+    } else if (is2d) {
         if (cfg.tile_x == 64) tile = 1;
         else if (cfg.tile_x == 256) tile = 2;
         else if (cfg.tile_x != 0 && cfg.tile_x != 128)
@@ -442,6 +468,17 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
         // FP32 rows: 256-wide strips (cp.async), 2-30 % over 128 on the
         // twelve reference shapes at 8192^2; float pairs keep 128
         if (cfg.tile_x == 0 && sp.dtype == UHS_F32 && arith != UHS_ARITH_DF32) tile = 2;
+        // Stars, two points per thread along x (vx 0 = planner's choice),
+        // GStencil/s per sweep at 8192^2 against the one-point default: in
+        // float pairs (packed sums) 128 columns by TMA, r1/r2/r3 366/253/184
+        // vs 310/214/163, or 256 by cp.async where TMA cannot load the grid
+        // (358/242/177); FP32 radius 2 by TMA 622 vs 581 (radius 1 even, 3
+        // slower).
+        if (cfg.tile_x == 0 && p->vx == 0 && shape == kStar2 && !(p->flags & UHS_FLAG_XSHUFFLE)) {
+            const bool tma = tma_aligned && cfg.use_tma >= 0;
+            if (arith == UHS_ARITH_DF32) tile = tma ? 3 : 4;
+            else if (sp.dtype == UHS_F32 && R == 2 && tma) tile = 3;
+        }
     } else if (cfg.tile_x == 0 && cfg.tile_y == 0 && p->vy == 0) {
         // Defaults from planner-against-exhaustive-tuning runs on GB300 at
         // 512^3 (studies.py shapes, reference and random coefficients).
@@ -489,6 +526,7 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
         const bool f32 = sp.dtype == UHS_F32 && arith == UHS_ARITH_FMA, f32x2 = sp.dtype == UHS_F32X2;
         if (!(is2d && shape == kStar2 && (f32 || f32x2)))
             return set_error(UHS_EUNSUPPORTED, "lane shuffles cover rank-2 stars on FP32 or float-pair grids");
+        if (p->vx == 2) return set_error(UHS_EUNSUPPORTED, "lane shuffles take one point per thread along x");
         const int want = f32 ? 2 : 0;
         if (cfg.tile_x != 0 && tile != want)
             return set_error(UHS_EUNSUPPORTED, "lane shuffles run %d-wide strips on this element type", f32 ? 256 : 128);
@@ -525,13 +563,13 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
         return UHS_OK;
     }
     // loader
-    const int eb = sp.dtype == UHS_F32 ? 4 : 8;
-    bool tma_ok = cfg.use_tma >= 0 && !(is2d && tile == 2);
+    bool tma_ok = cfg.use_tma >= 0 && !(is2d && (tile == 2 || tile == 4));
     // float-pair 2D boxes term by term load faster by cp.async (2d2r box at
     // 8192^2: 71.8 vs 65.6 GStencil/s with TMA)
     if (cfg.use_tma == 0 && is2d && shape == kBox2 && !sep && arith == UHS_ARITH_DF32) tma_ok = false;
-    const int64_t row_b = (is2d ? view.s[1] : view.s[1]) * eb, plane_b = (is2d ? view.s[1] : view.s[0]) * eb;
-    if (reinterpret_cast<uintptr_t>(view.data) % 16 || row_b % 16 || plane_b % 16) tma_ok = false;
+    if (!tma_aligned) tma_ok = false;
+    if (cfg.use_tma > 0 && is2d && (tile == 2 || tile == 4))
+        return set_error(UHS_EUNSUPPORTED, "256-column rank-2 tiles load by cp.async (a TMA box is at most 256 wide)");
     if (cfg.use_tma > 0 && !tma_ok)
         return set_error(UHS_EUNSUPPORTED, "TMA needs 16-byte aligned grids and row/plane strides");
     pl->ld = tma_ok ? kLdTma : kLdCpAsync;
@@ -780,6 +818,15 @@ static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in,
     c.xshuffle = pl.xshuffle ? 1 : 0;
     if (!c.err) return set_error(UHS_ENOMEM, "device error word allocation failed");
     const int eb = sp.dtype == UHS_F32 ? 4 : 8;
+    // two points per thread along x: start the tiles on an even element of
+    // the output's first row (vector stores of each thread's pair)
+    c.xoff = 0;
+    if (is2d && tile_shape(true, c.tile).vx == 2) {
+        const int64_t e0 = static_cast<int64_t>(reinterpret_cast<uintptr_t>(c.out.data) / eb) + c.lb[0] * c.out.s[0] +
+                           c.lb[2];
+        c.xoff = static_cast<int>(e0 & 1);
+    }
+    const int64_t tile_x0 = c.lb[2] - c.xoff;  // first column of the first tile
     CUtensorMap tmap;
     if (c.ld == kLdTma) {
         int W, H;
@@ -787,7 +834,7 @@ static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in,
         if (make_tmap(c.in, eb, W, H, &tmap)) {
             c.tmap = &tmap;
             const int q = 16 / eb;
-            c.shift = static_cast<int>(((c.lb[2] - c.R) % q + q) % q);
+            c.shift = static_cast<int>(((tile_x0 - c.R) % q + q) % q);
         } else {
             c.ld = kLdCpAsync;
         }
@@ -795,7 +842,7 @@ static int launch_sweep(const SweepSpec &sp, const Plan &pl, const GridView &in,
     c.zchunk = stream_zchunk(sp, pl, c, nullptr);
     // 4-byte grids: copy in 8-byte pairs when every row start of the tile is 8-byte aligned
     if (eb == 4 && c.ld == kLdCpAsync) {
-        const bool even = ((c.lb[2] - c.R) % 2 == 0) && c.in.s[0] % 2 == 0 && c.in.s[1] % 2 == 0 &&
+        const bool even = ((tile_x0 - c.R) % 2 == 0) && c.in.s[0] % 2 == 0 && c.in.s[1] % 2 == 0 &&
                           c.in.n[2] % 2 == 0 && reinterpret_cast<uintptr_t>(c.in.data) % 8 == 0;
         c.pair_loads = even ? 1 : 0;
     }
@@ -1119,8 +1166,7 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
                 return set_error(UHS_EUNSUPPORTED, "program %d is not a star/box stencil the batched kernel covers", i);
             if (pl.auto_df32 && descs[i].iterations > 0 &&
                 !range_ok(sp, va, vb, descs[i].iterations, scan_stream, &pl.pair_shift)) {
-                pl.ar = kArNative;
-                pl.cfg.arith = UHS_ARITH_FMA;
+                fall_back_native(pl);
             }
             const int nt = pl.factored ? 3 * (2 * pl.R + 1) : sp.nterms;
             const double per_term = pl.st == kStF32 ? 1.0 : pl.ar == kArDf32 ? 6.0 : 14.0;
@@ -1162,8 +1208,7 @@ static int batch_create(const uhs_stencil_desc *descs, const uhs_memref *as, con
             return set_error(UHS_EUNSUPPORTED, "program %d is not a star/box stencil the batched kernel covers", i);
         if (pl.auto_df32 && descs[i].iterations > 0 &&
             !range_ok(sp, va, vb, descs[i].iterations, scan_stream, &pl.pair_shift)) {
-            pl.ar = kArNative;
-            pl.cfg.arith = UHS_ARITH_FMA;
+            fall_back_native(pl);
         }
         int pack = kPackMain, kind = batch_kind(kPackMain, pl.shape, pl.R, pl.st, pl.ar);
         if (kind < 0) {
@@ -1467,7 +1512,7 @@ static bool tune_lookup(const uhs_stencil_desc *d, uhs_params *out, bool *exact)
 static bool params_are_auto(const uhs_params *p) {
     if (!p) return true;
     return p->kernel == 0 && p->arith == 0 && p->tile_x == 0 && p->tile_y == 0 && p->tile_z == 0 &&
-           p->k_temporal == 0 && p->use_tma == 0 && p->vy == 0 && p->prefetch == 0;
+           p->k_temporal == 0 && p->use_tma == 0 && p->vy == 0 && p->prefetch == 0 && p->vx == 0;
 }
 
 // The parameters a call runs with: the caller's, or the database's when the
@@ -1720,6 +1765,7 @@ int uhs_plan(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_params *p
         out->tile_x = bx;
         out->tile_y = sp.rank == 3 ? by : 1;
         out->vy = sp.rank == 3 ? tile_shape(false, (pl.shape == kBox3 && pl.R >= 2) ? 3 : pl.tile).vy : 1;
+        out->vx = sp.rank == 2 ? tile_shape(true, pl.tile).vx : 1;
         out->use_tma = pl.ld == kLdTma ? 1 : -1;
         out->factored = pl.factored ? 1 : 0;
         out->prefetch = pl.pd;
@@ -1774,8 +1820,7 @@ int uhs_sweep(const uhs_stencil_desc *d, const uhs_memref *in, const uhs_memref 
     if ((rc = plan_sweep(sp, p, vi, &pl))) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (pl.auto_df32 && !range_ok(sp, vi, vo, 1, st, &pl.pair_shift)) {
-        pl.ar = kArNative;
-        pl.cfg.arith = UHS_ARITH_FMA;
+        fall_back_native(pl);
     }
     if ((rc = launch_sweep(sp, pl, vi, vo, st))) return rc;
     return finish(p, st);
@@ -1794,8 +1839,7 @@ int uhs_run(const uhs_stencil_desc *d, const uhs_memref *a, const uhs_memref *b,
     if ((rc = plan_sweep(sp, p, va, &pl))) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (pl.auto_df32 && d->iterations > 0 && !range_ok(sp, va, vb, d->iterations, st, &pl.pair_shift)) {
-        pl.ar = kArNative;
-        pl.cfg.arith = UHS_ARITH_FMA;
+        fall_back_native(pl);
     }
     if (pl.kernel == UHS_KERNEL_STREAM && pl.cfg.k_temporal > 1 && d->iterations > 1) {
         bool eq = false;
@@ -1903,9 +1947,10 @@ int uhs_tune_get(const uhs_stencil_desc *d, uhs_params *out, int32_t *exact) {
     return UHS_OK;
 }
 
-// File format: a header line "uhs-tune 1", then one entry per line:
+// File format: a header line "uhs-tune 2", then one entry per line:
 //   rank shape R dtype ext0 ext1 ext2 kernel arith tile_x tile_y tile_z
-//   k_temporal use_tma flags vy prefetch gstencil_per_s
+//   k_temporal use_tma flags vy prefetch vx gstencil_per_s
+// (files of version 1, written before vx, have no vx column and still load)
 int uhs_tune_save(const char *path) {
     if (!path) return set_error(UHS_EINVAL, "path is NULL");
     std::map<TuneKey, TuneEntry> snap;
@@ -1916,14 +1961,15 @@ int uhs_tune_save(const char *path) {
     const std::string tmp = std::string(path) + ".tmp";
     FILE *f = std::fopen(tmp.c_str(), "w");
     if (!f) return set_error(UHS_EINVAL, "cannot write %s", tmp.c_str());
-    bool ok = std::fprintf(f, "uhs-tune 1\n") > 0;
+    bool ok = std::fprintf(f, "uhs-tune 2\n") > 0;
     for (const auto &kv : snap) {
         const TuneKey &k = kv.first;
         const uhs_params &q = kv.second.p;
-        ok = ok && std::fprintf(f, "%d %d %d %d %lld %lld %lld %d %d %d %d %d %d %d %d %d %d %.9g\n", k.rank, k.shape,
-                                k.R, k.dtype, static_cast<long long>(k.ext[0]), static_cast<long long>(k.ext[1]),
-                                static_cast<long long>(k.ext[2]), q.kernel, q.arith, q.tile_x, q.tile_y, q.tile_z,
-                                q.k_temporal, q.use_tma, q.flags, q.vy, q.prefetch, kv.second.gst) > 0;
+        ok = ok && std::fprintf(f, "%d %d %d %d %lld %lld %lld %d %d %d %d %d %d %d %d %d %d %d %.9g\n", k.rank,
+                                k.shape, k.R, k.dtype, static_cast<long long>(k.ext[0]),
+                                static_cast<long long>(k.ext[1]), static_cast<long long>(k.ext[2]), q.kernel, q.arith,
+                                q.tile_x, q.tile_y, q.tile_z, q.k_temporal, q.use_tma, q.flags, q.vy, q.prefetch, q.vx,
+                                kv.second.gst) > 0;
     }
     ok = (std::fclose(f) == 0) && ok;
     if (!ok || std::rename(tmp.c_str(), path) != 0) {
@@ -1944,10 +1990,13 @@ int uhs_tune_load(const char *path) {
     char line[512];
     int lineno = 0;
     int rc = UHS_OK;
+    int version = 0;
     while (std::fgets(line, sizeof line, f)) {
         ++lineno;
         if (lineno == 1) {
-            if (std::strncmp(line, "uhs-tune 1", 10) != 0) {
+            if (std::strncmp(line, "uhs-tune 1", 10) == 0) version = 1;
+            else if (std::strncmp(line, "uhs-tune 2", 10) == 0) version = 2;
+            else {
                 rc = set_error(UHS_EPARSE, "%s: not a tuner database (header)", path);
                 break;
             }
@@ -1960,9 +2009,17 @@ int uhs_tune_load(const char *path) {
         long long e0, e1, e2;
         double gst = 0.0;
         char extra[2];
-        const int n = std::sscanf(line, "%d %d %d %d %lld %lld %lld %d %d %d %d %d %d %d %d %d %d %lf %1s", &k.rank,
-                                  &k.shape, &k.R, &k.dtype, &e0, &e1, &e2, &q.kernel, &q.arith, &q.tile_x, &q.tile_y,
-                                  &q.tile_z, &q.k_temporal, &q.use_tma, &q.flags, &q.vy, &q.prefetch, &gst, extra);
+        int n;
+        if (version == 1) {
+            n = std::sscanf(line, "%d %d %d %d %lld %lld %lld %d %d %d %d %d %d %d %d %d %d %lf %1s", &k.rank, &k.shape,
+                            &k.R, &k.dtype, &e0, &e1, &e2, &q.kernel, &q.arith, &q.tile_x, &q.tile_y, &q.tile_z,
+                            &q.k_temporal, &q.use_tma, &q.flags, &q.vy, &q.prefetch, &gst, extra);
+        } else {
+            n = std::sscanf(line, "%d %d %d %d %lld %lld %lld %d %d %d %d %d %d %d %d %d %d %d %lf %1s", &k.rank,
+                            &k.shape, &k.R, &k.dtype, &e0, &e1, &e2, &q.kernel, &q.arith, &q.tile_x, &q.tile_y,
+                            &q.tile_z, &q.k_temporal, &q.use_tma, &q.flags, &q.vy, &q.prefetch, &q.vx, &gst, extra);
+            n -= 1;  // the vx column
+        }
         k.ext[0] = e0;
         k.ext[1] = e1;
         k.ext[2] = e2;
@@ -1974,7 +2031,8 @@ int uhs_tune_load(const char *path) {
                               q.arith >= UHS_ARITH_AUTO && q.arith <= UHS_ARITH_DF32 && q.tile_x >= 0 &&
                               q.tile_x <= 1024 && q.tile_y >= 0 && q.tile_y <= 1024 && q.tile_z >= 0 &&
                               q.k_temporal >= 0 && q.k_temporal <= 4 && q.use_tma >= -1 && q.use_tma <= 1 &&
-                              q.vy >= 0 && q.vy <= 8 && q.prefetch >= 0 && q.prefetch <= 8 && std::isfinite(gst);
+                              q.vy >= 0 && q.vy <= 8 && q.prefetch >= 0 && q.prefetch <= 8 && q.vx >= 0 &&
+                              q.vx <= 2 && std::isfinite(gst);
         if (!in_range) {
             rc = set_error(UHS_EPARSE, "%s:%d: malformed tuner entry", path, lineno);
             break;

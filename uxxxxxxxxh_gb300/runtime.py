@@ -27,16 +27,17 @@ class RunParams:
     vy: int = 0
     prefetch: int = 0
     factored: int = 0
+    vx: int = 0
 
     def to_c(self) -> _lib.Params:
         p = _lib.Params(self.kernel, self.arith, self.tile_x, self.tile_y, self.tile_z, self.k_temporal,
-                        self.use_tma, self.flags, self.vy, self.prefetch, self.factored)
+                        self.use_tma, self.flags, self.vy, self.prefetch, self.factored, self.vx)
         return p
 
     @staticmethod
     def from_c(p: _lib.Params) -> "RunParams":
         return RunParams(p.kernel, p.arith, p.tile_x, p.tile_y, p.tile_z, p.k_temporal, p.use_tma, p.flags, p.vy,
-                         p.prefetch, p.factored)
+                         p.prefetch, p.factored, p.vx)
 
 
 def memref_of(t, rank: int | None = None) -> _lib.Memref:

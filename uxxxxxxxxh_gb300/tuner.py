@@ -14,8 +14,9 @@ record for the learned cost model (costmodel.py).
 Candidates (rank 3): tile {32x32 VY4, 32x16 VY4, 64x8 VY2, 32x16 VY2, and for
 FP32 stars 32x32 VY8} x
 loader {TMA, cp.async} x z-chunk {auto, 16, 64} x arithmetic (FP64:
-{float pairs, native}); rank 2: rows {64, 128, 256} x loader x row chunk
-{auto, 64, 128} x arithmetic; plus the generic kernel, and on request
+{float pairs, native}); rank 2: rows {64, 128, 256} and, for stars on FP32
+grids or in float pairs, two points per thread along x over {128, 256}
+columns x loader x row chunk {auto, 64, 128} x arithmetic; plus the generic kernel, and on request
 (include_mma) for FP32 3D boxes of radius 2 and 3 the tensor-core kernel (16
 or 32 columns).  Candidates that plan to the same launch are timed once.
 """
@@ -34,6 +35,7 @@ from .stencil import Stencil
 STREAM, GENERIC, MMA = _lib.UHS_KERNEL_STREAM, _lib.UHS_KERNEL_GENERIC, _lib.UHS_KERNEL_MMA
 TILES3 = [(32, 32, 4), (32, 16, 4), (64, 8, 2), (32, 16, 2), (32, 32, 8)]
 TILES2 = [64, 128, 256]
+TILES2X = [128, 256]  # rank-2 stars, two points per thread along x (vx 2)
 
 
 def class_features(st: Stencil) -> list:
@@ -80,12 +82,14 @@ def config_features(p: RunParams, st: Stencil | None = None) -> list:
     arithmetic, z-chunk, generic kernel, and (given the program) how the tile
     quantises its domain: log2 CTA tiles and the idle fraction of edge tiles,
     and how the launch's CTAs fill the GPU (wave_features)."""
-    tile = [0.0] * (len(TILES3) + len(TILES2))
+    tile = [0.0] * (len(TILES3) + len(TILES2) + len(TILES2X))
     if p.kernel == STREAM:
         if p.tile_y > 1:
             key = (p.tile_x, p.tile_y, p.vy)
             if key in TILES3:
                 tile[TILES3.index(key)] = 1.0
+        elif p.vx == 2 and p.tile_x in TILES2X:
+            tile[len(TILES3) + len(TILES2) + TILES2X.index(p.tile_x)] = 1.0
         elif p.tile_x in TILES2:
             tile[len(TILES3) + TILES2.index(p.tile_x)] = 1.0
     quant = [0.0, 0.0, 0.0]
@@ -101,7 +105,7 @@ def config_features(p: RunParams, st: Stencil | None = None) -> list:
                    1.0 if p.kernel == MMA else 0.0] + quant + waves
 
 
-N_FEATURES = 9 + 19
+N_FEATURES = 9 + 21
 
 
 def features(st: Stencil, p: RunParams, cls: list | None = None) -> list:
@@ -117,7 +121,7 @@ def candidates(st: Stencil, include_mma: bool = False) -> list:
     ariths = [_lib.UHS_ARITH_DF32, _lib.UHS_ARITH_FMA] if st.dtype == _lib.UHS_F64 else \
         ([_lib.UHS_ARITH_DF32] if st.dtype == _lib.UHS_F32X2 else [_lib.UHS_ARITH_FMA])
     tiles = [dict(tile_x=t[0], tile_y=t[1], vy=t[2]) for t in TILES3] if st.rank == 3 else \
-        [dict(tile_x=t) for t in TILES2]
+        [dict(tile_x=t, vx=1) for t in TILES2] + [dict(tile_x=t, vx=2) for t in TILES2X]
     zs = [0, 16, 64] if st.rank == 3 else [0, 64, 128]
     raw = [RunParams(kernel=STREAM, arith=ar, use_tma=tma, tile_z=tz, flags=_lib.UHS_FLAG_NO_TUNE_DB, **t)
            for ar in ariths for t in tiles for tma in (1, -1) for tz in zs]
