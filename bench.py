@@ -88,7 +88,9 @@ NCU_BYTES_PER_POINT = {
     ("3d1r_star", "f32x2", "df32"): 15.34, ("3d1r_star", "f32", "fma"): 6.78,
     ("3d2r_star", "f32x2", "df32"): 15.97, ("3d2r_star", "f32", "fma"): 6.91,
     ("3d3r_box_sep", "f32x2", "df32"): 16.08, ("3d3r_box_sep", "f32", "fma"): 7.11,
-    ("2d1r_star", "f32x2", "df32"): 15.59, ("2d1r_star", "f32", "fma"): 7.35,
+    # rank-2 float-pair stars sweep two points per thread along x:
+    # profiles/k_stream_2d5pt_two_points_8192sq.md
+    ("2d1r_star", "f32x2", "df32"): 15.74, ("2d1r_star", "f32", "fma"): 7.35,
 }
 
 

@@ -734,9 +734,17 @@ static int stream_zchunk(const SweepSpec &sp, const Plan &pl, const StreamCall &
     int occ = 0;
     if (occ_out || (zchunk <= 0 && nz > 0 && tiles > 0)) occ = stream_occupancy(c);
     if (zchunk <= 0 && nz > 0 && tiles > 0) {
-        const int64_t want = static_cast<int64_t>(device_sms()) * occ * 4;
+        const int64_t slots = static_cast<int64_t>(device_sms()) * occ;
+        const int64_t want = slots * 4;
         const int64_t chunks = std::max<int64_t>(1, (want + tiles - 1) / tiles);
-        const int floor_z = std::max(sp.rank == 2 ? 32 : 8, 4 * c.R);
+        int floor_z = std::max(sp.rank == 2 ? 32 : 8, 4 * c.R);
+        // Float-pair rank-2 strips: 16-row chunks where those still make two
+        // waves (GStencil/s per sweep, 2d1r float pairs at 4096^2: 319 at 16
+        // rows vs 279 at 32, whose 1.1 waves leave most SMs idle in the
+        // second; at 3072^2, where 16 rows give 1.3 waves, 32 rows stay
+        // faster, 281 vs 239)
+        if (sp.rank == 2 && c.ar == kArDf32 && tiles * ((nz + 15) / 16) >= 2 * slots)
+            floor_z = std::max(16, 4 * c.R);
         zchunk = static_cast<int>(std::max<int64_t>(floor_z, (nz + chunks - 1) / chunks));
         if (pl.zcap > 0) zchunk = std::min(zchunk, std::max(pl.zcap, floor_z));
     }
