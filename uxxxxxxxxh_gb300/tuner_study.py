@@ -67,7 +67,7 @@ def draw_programs(n: int, seed: int, cover: bool = False, small: bool = False) -
 
 
 def run(n_train: int, n_test: int, reps: int, epochs: int, out: str | None, model_path: str | None,
-        seed: int = 101, n_small: int = 0) -> dict:
+        seed: int = 101, n_small: int = 0, net_seed: int | None = None) -> dict:
     t0 = time.time()
     tr = Tuner()
     for st in draw_programs(n_train, seed) + draw_programs(n_small, seed + 50, small=True):
@@ -75,7 +75,7 @@ def run(n_train: int, n_test: int, reps: int, epochs: int, out: str | None, mode
         tr.tune(st, a, b, reps=reps, push=False)
         del a, b
     t_collect = time.time() - t0
-    cm = CostModel(seed=seed)
+    cm = CostModel(seed=seed if net_seed is None else net_seed)
     t1 = time.time()
     loss = cm.fit(tr.records, epochs=epochs)
     t_train = time.time() - t1
@@ -135,8 +135,10 @@ def main():
     ap.add_argument("--epochs", type=int, default=300)
     ap.add_argument("--out", default=None)
     ap.add_argument("--model", default=None)
+    ap.add_argument("--net-seed", type=int, default=None,
+                    help="seed of the networks' initial weights and minibatch order (default: the program seed)")
     a = ap.parse_args()
-    res = run(a.train, a.test, a.reps, a.epochs, a.out, a.model, n_small=a.small)
+    res = run(a.train, a.test, a.reps, a.epochs, a.out, a.model, n_small=a.small, net_seed=a.net_seed)
     print(json.dumps({k: v for k, v in res.items() if k != "rows"}))
 
 
