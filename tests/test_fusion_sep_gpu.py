@@ -52,9 +52,13 @@ def test_fused_rejects_different_halos_and_other_shapes(cuda):
     with pytest.raises(uhs.UhsError) as ei:
         run_gpu(st, a0, uhs.RunParams(k_temporal=2), b0=b0)
     assert ei.value.code == uhs._lib.UHS_EINVAL
+    # depth 4 of a radius-2 3D star does not fit shared memory; float-pair grids are not fused
     st2, _ = random_case(3, 2, "star", (10, 10, 40), 4, 35)
+    uhs.plan(st2, params=uhs.RunParams(k_temporal=2))
     with pytest.raises(uhs.UhsError):
-        uhs.plan(st2, params=uhs.RunParams(k_temporal=2))
+        uhs.plan(st2, params=uhs.RunParams(k_temporal=4))
+    with pytest.raises(uhs.UhsError):
+        uhs.plan(st.with_(dtype=uhs._lib.UHS_F32X2), params=uhs.RunParams(k_temporal=2))
 
 
 @pytest.mark.parametrize("case", ["3d1r_box", "3d2r_box", "3d3r_box", "2d2r_box", "2d3r_box"])

@@ -166,3 +166,24 @@ def test_two_points_along_x_is_for_rank2_stars():
             plan(bad, memref_raw(1 << 20, bad.sizes), params=RunParams(vx=2, **kw))
     with pytest.raises(F.UhsError):
         plan(st, raw, params=RunParams(vx=3, flags=F.UHS_FLAG_NO_TUNE_DB))
+
+
+def test_temporal_fusion_planning():
+    """k_temporal 2 and 4 plan for every star and box shape of rank 2 and
+    radius-1 shapes of rank 3 (depth 2 for radius 2-3 in 3D); fused boxes are
+    summed term by term (not factored); float-pair grids and two points per
+    thread along x are refused."""
+    for rank, r, kind in [(2, 3, "box"), (2, 1, "star"), (3, 1, "box"), (3, 3, "star")]:
+        st, _ = random_case(rank, r, kind, (40, 300) if rank == 2 else (20, 20, 40), 4, 3)
+        for k in ((2, 4) if rank == 2 or r == 1 else (2,)):
+            p = plan(st, memref_raw(1 << 20, st.sizes), params=RunParams(k_temporal=k, flags=F.UHS_FLAG_NO_TUNE_DB))
+            assert (p.k_temporal, p.factored, p.prefetch) == (k, 0, 2)
+    st, _ = random_case(3, 2, "box", (20, 20, 40), 4, 3)
+    with pytest.raises(F.UhsError):
+        plan(st, memref_raw(1 << 20, st.sizes), params=RunParams(k_temporal=4, flags=F.UHS_FLAG_NO_TUNE_DB))
+    st, _ = random_case(2, 1, "star", (40, 300), 4, 3)
+    for bad in (dict(vx=2), dict(k_temporal=3)):
+        with pytest.raises(F.UhsError):
+            plan(st, memref_raw(1 << 20, st.sizes), params=RunParams(**{"k_temporal": 2, **bad}))
+    with pytest.raises(F.UhsError):
+        plan(st.with_(dtype=F.UHS_F32X2), memref_raw(1 << 20, st.sizes), params=RunParams(k_temporal=2))

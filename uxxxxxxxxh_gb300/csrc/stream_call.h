@@ -169,6 +169,7 @@ cudaError_t batch_launch(int pack, const BatchGrid *grids, const int4 *items, in
 // Temporal fusion (stream_fused.cu): K in {2, 4} steps of the 3D 7-point
 // star per pass; and the halo comparison that gates it.
 cudaError_t launch_fused(const StreamCall &c, int K);
+cudaError_t launch_fused_2d(const StreamCall &c, int K);  // stream_fused_2d.cu
 cudaError_t launch_halo_diff(const GridView &a, const GridView &b, int eb, const int64_t lb[3], const int64_t ub[3],
                              unsigned *count, int sms, cudaStream_t st);
 

@@ -431,8 +431,16 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
         cfg.kernel = kernel;
         return UHS_OK;
     }
-    if (cfg.k_temporal > 1 && !(shape == kStar3 && R == 1 && sp.dtype != UHS_F32X2))
-        return set_error(UHS_EUNSUPPORTED, "temporal fusion covers the 3D 7-point star on FP32/FP64 grids");
+    // temporal fusion (stream_fused.cuh): star and box stencils on FP32/FP64
+    // grids, depths 2 and 4 (4 in 3D for radius 1 only: deeper 3D tiles of
+    // radius 2-3 do not fit shared memory)
+    if (cfg.k_temporal > 1) {
+        if (sp.dtype == UHS_F32X2)
+            return set_error(UHS_EUNSUPPORTED, "temporal fusion covers FP32 and FP64 grids (not float-pair grids)");
+        if (cfg.k_temporal == 4 && sp.rank == 3 && R > 1)
+            return set_error(UHS_EUNSUPPORTED, "temporal fusion of depth 4 covers radius 1 in 3D (depth 2 for radius %d)", R);
+        if (p->vx == 2) return set_error(UHS_EUNSUPPORTED, "temporal fusion takes one point per thread along x");
+    }
     pl->kernel = cfg.kernel = UHS_KERNEL_STREAM;
     pl->shape = shape;
     pl->R = R;
@@ -441,7 +449,9 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
     const bool is2d = sp.rank == 2;
     // separable boxes run as 1D passes unless the caller opts out
     std::vector<double> fac;
-    const bool sep = (shape == kBox3 || shape == kBox2) && !(p->flags & UHS_FLAG_NO_FACTOR) && factor_box(sp, R, &fac);
+    // (fused passes sum boxes term by term)
+    const bool sep = (shape == kBox3 || shape == kBox2) && !(p->flags & UHS_FLAG_NO_FACTOR) && cfg.k_temporal <= 1 &&
+                     factor_box(sp, R, &fac);
     // whether the grid allows TMA loads: 16-byte aligned base, row and plane pitches
     const int eb = sp.dtype == UHS_F32 ? 4 : 8;
     const int64_t row_b = view.s[1] * eb, plane_b = (is2d ? view.s[1] : view.s[0]) * eb;
@@ -537,7 +547,7 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
     // Load-ahead depth: built into each variant (2D strips 4 rows; 3D 3
     // planes, 2 for radius 2-3 boxes swept term by term; temporal fusion 2).
     // A caller may state it, not choose another.
-    pl->pd = is2d ? 4 : cfg.k_temporal > 1 ? 2 : (shape == kBox3 && R >= 2 && !sep) ? 2 : 3;
+    pl->pd = cfg.k_temporal > 1 ? 2 : is2d ? 4 : (shape == kBox3 && R >= 2 && !sep) ? 2 : 3;
     if (p->prefetch != 0 && p->prefetch != pl->pd)
         return set_error(UHS_EUNSUPPORTED, "this streaming variant loads %d %s ahead (prefetch %d)", pl->pd,
                          is2d ? "rows" : "planes", p->prefetch);
@@ -913,20 +923,27 @@ static int launch_fused_pass(const SweepSpec &sp, const Plan &pl, const GridView
     c.st = pl.st;
     c.ar = pl.ar;
     c.coef = pl.coef.data();
-    c.in = in;
-    c.out = out;
-    for (int i = 0; i < 3; ++i) {
-        c.lb[i] = sp.lb[i];
-        c.ub[i] = sp.ub[i];
-    }
+    // the kernel's (z, y, x) frame: rank-2 rows stream as planes
+    const bool is2d = sp.rank == 2;
+    c.in = kernel_view(sp, in);
+    c.out = kernel_view(sp, out);
+    c.lb[0] = is2d ? sp.lb[1] : sp.lb[0];
+    c.ub[0] = is2d ? sp.ub[1] : sp.ub[0];
+    c.lb[1] = is2d ? 0 : sp.lb[1];
+    c.ub[1] = is2d ? 1 : sp.ub[1];
+    c.lb[2] = sp.lb[2];
+    c.ub[2] = sp.ub[2];
     c.stream = st;
     int dev = 0;
     cudaGetDevice(&dev);
     c.err = stream_error_word(dev, st);
     if (!c.err) return set_error(UHS_ENOMEM, "device error word allocation failed");
     c.pair_shift = pl.pair_shift;
-    const int64_t nz = sp.ub[0] - sp.lb[0];
-    const int64_t tiles = ((sp.ub[2] - sp.lb[2] + 31) / 32) * ((sp.ub[1] - sp.lb[1] + 15) / 16);
+    // output tile of the fused kernel: 256 - 2KR columns of a row (2D),
+    // 32 x 16 (radius 1) or 32 x 8 cells (3D)
+    const int bx = is2d ? 256 - 2 * K * pl.R : 32, by = is2d ? 1 : (pl.R >= 2 ? 8 : 16);
+    const int64_t nz = c.ub[0] - c.lb[0];
+    const int64_t tiles = ((c.ub[2] - c.lb[2] + bx - 1) / bx) * ((c.ub[1] - c.lb[1] + by - 1) / by);
     int zchunk = pl.cfg.tile_z;
     if (zchunk <= 0 && nz > 0 && tiles > 0) {
         int occ = 0;
@@ -935,7 +952,7 @@ static int launch_fused_pass(const SweepSpec &sp, const Plan &pl, const GridView
         if (launch_fused(q, K) != cudaSuccess || occ <= 0) occ = 1;
         const int64_t want = static_cast<int64_t>(device_sms()) * occ * 3;
         const int64_t chunks = std::max<int64_t>(1, (want + tiles - 1) / tiles);
-        zchunk = static_cast<int>(std::max<int64_t>(8 * K, (nz + chunks - 1) / chunks));
+        zchunk = static_cast<int>(std::max<int64_t>(8 * K * pl.R, (nz + chunks - 1) / chunks));
     }
     c.zchunk = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(zchunk, std::max<int64_t>(nz, 1))));
     cudaError_t e = launch_fused(c, K);
