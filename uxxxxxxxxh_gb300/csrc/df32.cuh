@@ -197,3 +197,87 @@ __device__ __forceinline__ void renorm2(const df2 &a, u64 &h, u64 &l) {
 }
 
 }  // namespace uhs
+
+namespace uhs {
+
+// ---- bounded sums: one stencil point's sum with an extraction bound ---------
+// A point's sum  s = sum_k c_k * x_k  (float pairs c = ch + cl, x = xh + xl)
+// in fewer FP32 operations than df_fma's TwoSum per term, by extracting each
+// product's high part on a fixed grid (Rump, Ogita and Oishi, "Accurate
+// floating-point summation", ExtractScalar):
+//   B = sum_k |ch_k| |xh_k| (one FMA per term, bound_add);
+//   sigma = 2^m, B (1 + 2^-16) < sigma <= 2 B (1 + 2^-16) (sigma_of);
+//   p = ch * xh;  q = (sigma + p) - sigma;  r = fma(ch, xh, -q)
+// With |p| <= sigma, q is p on the grid of multiples of 2^-24 sigma and
+// p - q is exact (ExtractScalar's lemma), so every partial sum of the q's --
+// multiples of 2^-24 sigma below sigma in magnitude, as sum |p| and the n
+// roundings to the grid stay below B (1 + (2n + 1) 2^-24) < sigma for up to
+// 127 terms -- is exact in a float: tau = sum q_k carries no error.  r is
+// the rest of the exact product, ch * xh - q, rounded once (|r| <= 2^-23
+// sigma, so its error is below 2^-47 sigma), and the low-order parts go into
+// lo:
+//   lo += r;  lo = fma(ch, xl, lo);  lo = fma(cl, xh, lo)
+// 9 FP32 operations per term with the bound, against df_fma's 12.  The
+// point's value is tau + lo, renormalised by one TwoSum (renorm) as before.
+// The error is relative to sum |c_k x_k| of the point itself, as with
+// df_fma's errors relative to its partial sums: lo sums n terms of at most
+// 2^-23 sigma <= 2^-22 (1 + 2^-16) B, so its roundings stay below about
+// n^2 2^-46 B, in practice (random signs) near n^1.5 2^-47 B; for a field of
+// one sign, B is the point's value.
+//
+// The bound's exponent is clamped so sigma stays a normal float (inputs
+// beyond 2^125 overflow the grid: the range flag catches them).
+__device__ __forceinline__ float bound_add(float b, float ch, float2 x) {
+    return __fmaf_rn(fabsf(ch), fabsf(x.x), b);
+}
+__device__ __forceinline__ float sigma_of(float b) {
+    const float bb = __fmul_ru(b, 1.0000152587890625f);  // 1 + 2^-16
+    const int e = min(static_cast<int>(__float_as_uint(bb) & 0x7f800000u), 253 << 23);
+    return __int_as_float(e + (1 << 23));
+}
+
+// acc = c * x (first term of a bounded sum)
+__device__ __forceinline__ void dfs_mul(df &acc, float sigma, float ch, float cl, float2 x) {
+    const float p = __fmul_rn(ch, x.x);
+    const float q = __fsub_rn(__fadd_rn(sigma, p), sigma);
+    const float r = __fmaf_rn(ch, x.x, -q);
+    acc.h = q;
+    acc.l = __fmaf_rn(cl, x.x, __fmaf_rn(ch, x.y, r));
+}
+
+// acc += c * x (bounded sum)
+__device__ __forceinline__ void dfs_fma(df &acc, float sigma, float ch, float cl, float2 x) {
+    const float p = __fmul_rn(ch, x.x);
+    const float q = __fsub_rn(__fadd_rn(sigma, p), sigma);
+    const float r = __fmaf_rn(ch, x.x, -q);
+    acc.h = __fadd_rn(acc.h, q);
+    acc.l = __fmaf_rn(cl, x.x, __fmaf_rn(ch, x.y, __fadd_rn(acc.l, r)));
+}
+
+// The same for two points at once: the extraction and the two additions
+// packed (.f32x2), the products and the low-order terms per point.  Per
+// point the same operations as dfs_mul / dfs_fma, so bit-identical to them.
+// sig holds {sigma of point 0, sigma of point 1}.
+__device__ __forceinline__ void dfs2_mul_s(df2 &acc, u64 sig, float ch, float cl, float2 x0, float2 x1) {
+    const u64 p = pk2(__fmul_rn(ch, x0.x), __fmul_rn(ch, x1.x));
+    const u64 q = sub2(add2(sig, p), sig);
+    float q0, q1;
+    upk2(q, q0, q1);
+    const float r0 = __fmaf_rn(ch, x0.x, -q0), r1 = __fmaf_rn(ch, x1.x, -q1);
+    acc.h = q;
+    acc.l = pk2(__fmaf_rn(cl, x0.x, __fmaf_rn(ch, x0.y, r0)), __fmaf_rn(cl, x1.x, __fmaf_rn(ch, x1.y, r1)));
+}
+
+__device__ __forceinline__ void dfs2_fma_s(df2 &acc, u64 sig, float ch, float cl, float2 x0, float2 x1) {
+    const u64 p = pk2(__fmul_rn(ch, x0.x), __fmul_rn(ch, x1.x));
+    const u64 q = sub2(add2(sig, p), sig);
+    float q0, q1;
+    upk2(q, q0, q1);
+    const float r0 = __fmaf_rn(ch, x0.x, -q0), r1 = __fmaf_rn(ch, x1.x, -q1);
+    acc.h = add2(acc.h, q);
+    float l0, l1;
+    upk2(add2(acc.l, pk2(r0, r1)), l0, l1);
+    acc.l = pk2(__fmaf_rn(cl, x0.x, __fmaf_rn(ch, x0.y, l0)), __fmaf_rn(cl, x1.x, __fmaf_rn(ch, x1.y, l1)));
+}
+
+}  // namespace uhs

@@ -262,6 +262,16 @@ struct Arith<C, kArNative> {
         if constexpr (F32) acc = fmaf(a.cl_sum[pass], v, acc);
     }
     __device__ static __forceinline__ void store(TS *p, const Acc &acc, unsigned &, int) { *p = acc; }
+    // bounded sums (float pairs only): the plain sum here
+    static constexpr bool kBounded = false;
+    template <class Args>
+    __device__ static __forceinline__ void bfirst(Acc &acc, float, const Args &a, int k, TS v) {
+        first(acc, a, k, v);
+    }
+    template <class Args>
+    __device__ static __forceinline__ void badd(Acc &acc, float, const Args &a, int k, TS v) {
+        add(acc, a, k, v);
+    }
     // two adjacent points, p aligned to 2 * sizeof(TS)
     static constexpr bool kVecStore = true;
     __device__ static __forceinline__ void store2(TS *p, const Acc &a0, const Acc &a1, unsigned &, int) {
@@ -283,6 +293,19 @@ struct Arith<C, kArDf32> {
     __device__ static __forceinline__ void add(Acc &acc, const Args &a, int k, float2 v) {
         const float2 c = coef_f2<C>(a, k);
         df_fma(acc, c.x, c.y, v);
+    }
+    // Star and separable sums: bounded sums (dfs_mul / dfs_fma in df32.cuh),
+    // sg = the point's sigma_of.  Term-by-term boxes keep first / add.
+    static constexpr bool kBounded = true;
+    template <class Args>
+    __device__ static __forceinline__ void bfirst(Acc &acc, float sg, const Args &a, int k, float2 v) {
+        const float2 c = coef_f2<C>(a, k);
+        dfs_mul(acc, sg, c.x, c.y, v);
+    }
+    template <class Args>
+    __device__ static __forceinline__ void badd(Acc &acc, float sg, const Args &a, int k, float2 v) {
+        const float2 c = coef_f2<C>(a, k);
+        dfs_fma(acc, sg, c.x, c.y, v);
     }
     // FP64 grids: joined back with the run's exponent bias (the pairs hold
     // x * 2^pair_shift).  A sum that outgrew the float range (hi Inf or NaN)
@@ -312,6 +335,34 @@ struct Arith<C, kArDf32> {
     template <class Args>
     __device__ static __forceinline__ void centre(Acc &, const Args &, int, float2) {}
 };
+
+// Bound B of a star point's bounded sum (df32.cuh): sum |ch_k| |xh_k| over
+// its inputs in the sum's order -- centre, +-d along z, y (rank 3), x.
+// zq: the point's z-queue (centre at [R]); col: its y column (centre at
+// [R]); row: its row in shared memory (centre at [0]).
+template <class C, class Args, class TC>
+__device__ __forceinline__ float star_bound(const Args &a, const TC *zq, const TC *col, const TC *row) {
+    constexpr int R = C::R;
+    float b = bound_add(0.0f, coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, 0, 0)).x, zq[R]);
+#pragma unroll
+    for (int d = 1; d <= R; ++d) {
+        b = bound_add(b, coef_f2<C>(a, coef_slot<C::SHAPE, R>(-d, 0, 0)).x, zq[R - d]);
+        b = bound_add(b, coef_f2<C>(a, coef_slot<C::SHAPE, R>(d, 0, 0)).x, zq[R + d]);
+    }
+    if constexpr (!C::SI::is2d) {
+#pragma unroll
+        for (int d = 1; d <= R; ++d) {
+            b = bound_add(b, coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, -d, 0)).x, col[R - d]);
+            b = bound_add(b, coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, d, 0)).x, col[R + d]);
+        }
+    }
+#pragma unroll
+    for (int d = 1; d <= R; ++d) {
+        b = bound_add(b, coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, 0, -d)).x, row[-d]);
+        b = bound_add(b, coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, 0, d)).x, row[d]);
+    }
+    return b;
+}
 
 // ---- the kernel ---------------------------------------------------------
 // One work item: the (bx, by) tile of the (y, x) plane over z-chunk bz.
@@ -556,13 +607,21 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
 #pragma unroll
             for (int i = 0; i < NROW; i += 2) {
                 const TC *r0 = cur + own + (i - R) * W, *r1 = r0 + W;
+                float b0 = 0.0f, b1 = 0.0f;
+#pragma unroll
+                for (int dx = -R; dx <= R; ++dx) {
+                    const float ch = coef_f2<C>(a, CX0 + dx + R).x;
+                    b0 = bound_add(b0, ch, r0[dx]);
+                    b1 = bound_add(b1, ch, r1[dx]);
+                }
+                const u64 sg = pk2(sigma_of(b0), sigma_of(b1));
                 df2 t;
                 float2 c = coef_f2<C>(a, CX0);
-                df2_mul_s(t, c.x, c.y, r0[-R], r1[-R]);
+                dfs2_mul_s(t, sg, c.x, c.y, r0[-R], r1[-R]);
 #pragma unroll
                 for (int dx = -R + 1; dx <= R; ++dx) {
                     c = coef_f2<C>(a, CX0 + dx + R);
-                    df2_fma_s(t, c.x, c.y, r0[dx], r1[dx]);
+                    dfs2_fma_s(t, sg, c.x, c.y, r0[dx], r1[dx]);
                 }
                 u64 hh, ll;
                 renorm2(t, hh, ll);
@@ -576,13 +635,21 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                     q[v][k] = q[v][k + 1];
                     q[v + 1][k] = q[v + 1][k + 1];
                 }
+                float b0 = 0.0f, b1 = 0.0f;
+#pragma unroll
+                for (int dy = -R; dy <= R; ++dy) {
+                    const float ch = coef_f2<C>(a, D + dy + R).x;
+                    b0 = bound_add(b0, ch, xr[v + R + dy]);
+                    b1 = bound_add(b1, ch, xr[v + 1 + R + dy]);
+                }
+                const u64 sg = pk2(sigma_of(b0), sigma_of(b1));
                 df2 t;
                 float2 c = coef_f2<C>(a, D);
-                df2_mul_s(t, c.x, c.y, xr[v], xr[v + 1]);
+                dfs2_mul_s(t, sg, c.x, c.y, xr[v], xr[v + 1]);
 #pragma unroll
                 for (int dy = -R + 1; dy <= R; ++dy) {
                     c = coef_f2<C>(a, D + dy + R);
-                    df2_fma_s(t, c.x, c.y, xr[v + R + dy], xr[v + 1 + R + dy]);
+                    dfs2_fma_s(t, sg, c.x, c.y, xr[v + R + dy], xr[v + 1 + R + dy]);
                 }
                 u64 hh, ll;
                 renorm2(t, hh, ll);
@@ -600,10 +667,17 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
 #pragma unroll
             for (int i = 0; i < NROW; ++i) {
                 const TC *row = cur + own + (IS2D ? 0 : (i - R) * W);
-                Acc t;
-                A::first(t, a, CX0, row[-R]);
+                float sg = 0.0f;
+                if constexpr (A::kBounded) {
+                    float b = 0.0f;
 #pragma unroll
-                for (int dx = -R + 1; dx <= R; ++dx) A::add(t, a, CX0 + dx + R, row[dx]);
+                    for (int dx = -R; dx <= R; ++dx) b = bound_add(b, coef_f2<C>(a, CX0 + dx + R).x, row[dx]);
+                    sg = sigma_of(b);
+                }
+                Acc t;
+                A::bfirst(t, sg, a, CX0, row[-R]);
+#pragma unroll
+                for (int dx = -R + 1; dx <= R; ++dx) A::badd(t, sg, a, CX0 + dx + R, row[dx]);
                 A::centre(t, a, IS2D ? 1 : 2, row[0]);
                 xr[i] = A::level(t);
             }
@@ -614,10 +688,17 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                 if constexpr (IS2D) {
                     q[v][2 * R] = xr[0];
                 } else {
-                    Acc t;
-                    A::first(t, a, D, xr[v]);
+                    float sg = 0.0f;
+                    if constexpr (A::kBounded) {
+                        float b = 0.0f;
 #pragma unroll
-                    for (int dy = -R + 1; dy <= R; ++dy) A::add(t, a, D + dy + R, xr[v + R + dy]);
+                        for (int dy = -R; dy <= R; ++dy) b = bound_add(b, coef_f2<C>(a, D + dy + R).x, xr[v + R + dy]);
+                        sg = sigma_of(b);
+                    }
+                    Acc t;
+                    A::bfirst(t, sg, a, D, xr[v]);
+#pragma unroll
+                    for (int dy = -R + 1; dy <= R; ++dy) A::badd(t, sg, a, D + dy + R, xr[v + R + dy]);
                     A::centre(t, a, 1, xr[v + R]);
                     q[v][2 * R] = A::level(t);
                 }
@@ -640,21 +721,47 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                 if constexpr (SEP) {
 #pragma unroll
                     for (int p = 0; p < NPR; ++p) {
+                        float b0 = 0.0f, b1 = 0.0f;
+#pragma unroll
+                        for (int dz = 0; dz < 2 * R + 1; ++dz) {
+                            const float ch = coef_f2<C>(a, dz).x;
+                            b0 = bound_add(b0, ch, q[2 * p][dz]);
+                            b1 = bound_add(b1, ch, q[2 * p + 1][dz]);
+                        }
+                        const u64 sg = pk2(sigma_of(b0), sigma_of(b1));
                         float2 c = coef_f2<C>(a, 0);
-                        df2_mul_s(acc[p], c.x, c.y, q[2 * p][0], q[2 * p + 1][0]);
+                        dfs2_mul_s(acc[p], sg, c.x, c.y, q[2 * p][0], q[2 * p + 1][0]);
 #pragma unroll
                         for (int dz = 1; dz < 2 * R + 1; ++dz) {
                             c = coef_f2<C>(a, dz);
-                            df2_fma_s(acc[p], c.x, c.y, q[2 * p][dz], q[2 * p + 1][dz]);
+                            dfs2_fma_s(acc[p], sg, c.x, c.y, q[2 * p][dz], q[2 * p + 1][dz]);
                         }
                     }
                 } else if constexpr (STAR) {
                     const int sl = slot_j >= R ? slot_j - R : slot_j - R + NRING;
                     const TC *pl = cmp_base + sl * CMP_STRIDE;
+                    // the y column (rank 3) and each point's sigma from all its inputs
+                    TC col[IS2D ? 1 : VY + 2 * R];
+                    if constexpr (!IS2D) {
+#pragma unroll
+                        for (int i = 0; i < VY + 2 * R; ++i) col[i] = pl[own + (i - R) * W];
+                    }
+                    u64 sg[NPR];
+#pragma unroll
+                    for (int p = 0; p < NPR; ++p) {
+                        float b[2];
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            const int v = 2 * p + h;
+                            const TC *row = pl + own + v * PSTEP;
+                            b[h] = star_bound<C>(a, q[v], col + v, row);
+                        }
+                        sg[p] = pk2(sigma_of(b[0]), sigma_of(b[1]));
+                    }
 #pragma unroll
                     for (int p = 0; p < NPR; ++p) {
                         const float2 c = coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, 0, 0));
-                        df2_mul_s(acc[p], c.x, c.y, q[2 * p][R], q[2 * p + 1][R]);
+                        dfs2_mul_s(acc[p], sg[p], c.x, c.y, q[2 * p][R], q[2 * p + 1][R]);
                     }
 #pragma unroll
                     for (int d = 1; d <= R; ++d)
@@ -662,21 +769,18 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                         for (int p = 0; p < NPR; ++p) {
                             const float2 cm = coef_f2<C>(a, coef_slot<C::SHAPE, R>(-d, 0, 0));
                             const float2 cp = coef_f2<C>(a, coef_slot<C::SHAPE, R>(d, 0, 0));
-                            df2_fma_s(acc[p], cm.x, cm.y, q[2 * p][R - d], q[2 * p + 1][R - d]);
-                            df2_fma_s(acc[p], cp.x, cp.y, q[2 * p][R + d], q[2 * p + 1][R + d]);
+                            dfs2_fma_s(acc[p], sg[p], cm.x, cm.y, q[2 * p][R - d], q[2 * p + 1][R - d]);
+                            dfs2_fma_s(acc[p], sg[p], cp.x, cp.y, q[2 * p][R + d], q[2 * p + 1][R + d]);
                         }
                     if constexpr (!IS2D) {
-                        TC col[VY + 2 * R];
-#pragma unroll
-                        for (int i = 0; i < VY + 2 * R; ++i) col[i] = pl[own + (i - R) * W];
 #pragma unroll
                         for (int d = 1; d <= R; ++d)
 #pragma unroll
                             for (int p = 0; p < NPR; ++p) {
                                 const float2 cm = coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, -d, 0));
                                 const float2 cp = coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, d, 0));
-                                df2_fma_s(acc[p], cm.x, cm.y, col[2 * p + R - d], col[2 * p + 1 + R - d]);
-                                df2_fma_s(acc[p], cp.x, cp.y, col[2 * p + R + d], col[2 * p + 1 + R + d]);
+                                dfs2_fma_s(acc[p], sg[p], cm.x, cm.y, col[2 * p + R - d], col[2 * p + 1 + R - d]);
+                                dfs2_fma_s(acc[p], sg[p], cp.x, cp.y, col[2 * p + R + d], col[2 * p + 1 + R + d]);
                             }
                     }
 #pragma unroll
@@ -686,8 +790,8 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                             const TC *r0 = pl + own + 2 * p * PSTEP, *r1 = r0 + PSTEP;
                             const float2 cm = coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, 0, -d));
                             const float2 cp = coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, 0, d));
-                            df2_fma_s(acc[p], cm.x, cm.y, r0[-d], r1[-d]);
-                            df2_fma_s(acc[p], cp.x, cp.y, r0[d], r1[d]);
+                            dfs2_fma_s(acc[p], sg[p], cm.x, cm.y, r0[-d], r1[-d]);
+                            dfs2_fma_s(acc[p], sg[p], cp.x, cp.y, r0[d], r1[d]);
                         }
                 } else {
 #pragma unroll
@@ -747,38 +851,29 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
             if constexpr (SEP) {
 #pragma unroll
                 for (int v = 0; v < VY; ++v) {
-                    A::first(acc[v], a, 0, q[v][0]);
+                    float sg = 0.0f;
+                    if constexpr (A::kBounded) {
+                        float b = 0.0f;
 #pragma unroll
-                    for (int dz = 1; dz < 2 * R + 1; ++dz) A::add(acc[v], a, dz, q[v][dz]);
+                        for (int dz = 0; dz < 2 * R + 1; ++dz) b = bound_add(b, coef_f2<C>(a, dz).x, q[v][dz]);
+                        sg = sigma_of(b);
+                    }
+                    A::bfirst(acc[v], sg, a, 0, q[v][0]);
+#pragma unroll
+                    for (int dz = 1; dz < 2 * R + 1; ++dz) A::badd(acc[v], sg, a, dz, q[v][dz]);
                     A::centre(acc[v], a, 0, q[v][R]);
                 }
             } else if constexpr (STAR) {
                 const int sl = slot_j >= R ? slot_j - R : slot_j - R + NRING;
                 const TC *pl = cmp_base + sl * CMP_STRIDE;
-#pragma unroll
-                for (int v = 0; v < NPT; ++v) {
-                    A::first(acc[v], a, coef_slot<C::SHAPE, R>(0, 0, 0), q[v][R]);
-                    A::centre(acc[v], a, 0, q[v][R]);
-                }
-#pragma unroll
-                for (int d = 1; d <= R; ++d)
-#pragma unroll
-                    for (int v = 0; v < NPT; ++v) {
-                        A::add(acc[v], a, coef_slot<C::SHAPE, R>(-d, 0, 0), q[v][R - d]);
-                        A::add(acc[v], a, coef_slot<C::SHAPE, R>(d, 0, 0), q[v][R + d]);
-                    }
+                // every input of each point first: the y column (rank 3) and
+                // the x-neighbours, xn[v][d - 1] = {x - d, x + d}
+                TC col[IS2D ? 1 : VY + 2 * R];
                 if constexpr (!IS2D) {
-                    TC col[VY + 2 * R];
 #pragma unroll
                     for (int i = 0; i < VY + 2 * R; ++i) col[i] = pl[own + (i - R) * W];
-#pragma unroll
-                    for (int d = 1; d <= R; ++d)
-#pragma unroll
-                        for (int v = 0; v < VY; ++v) {
-                            A::add(acc[v], a, coef_slot<C::SHAPE, R>(0, -d, 0), col[v + R - d]);
-                            A::add(acc[v], a, coef_slot<C::SHAPE, R>(0, d, 0), col[v + R + d]);
-                        }
                 }
+                TC xn[NPT][R][2];
                 if constexpr (IS2D && C::XS) {
                     // x-neighbours from the lanes d columns away (the warp's
                     // lanes hold consecutive columns; their centre values are
@@ -791,19 +886,63 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                         TC lft = shfl_up_tc(cen, d), rgt = shfl_down_tc(cen, d);
                         if (lane < d) lft = row[-d];
                         if (lane >= 32 - d) rgt = row[d];
-                        A::add(acc[0], a, coef_slot<C::SHAPE, R>(0, 0, -d), lft);
-                        A::add(acc[0], a, coef_slot<C::SHAPE, R>(0, 0, d), rgt);
+                        xn[0][d - 1][0] = lft;
+                        xn[0][d - 1][1] = rgt;
                     }
                 } else {
 #pragma unroll
+                    for (int v = 0; v < NPT; ++v) {
+                        const TC *row = pl + own + v * PSTEP;
+#pragma unroll
+                        for (int d = 1; d <= R; ++d) {
+                            xn[v][d - 1][0] = row[-d];
+                            xn[v][d - 1][1] = row[d];
+                        }
+                    }
+                }
+                float sg[NPT];
+#pragma unroll
+                for (int v = 0; v < NPT; ++v) {
+                    sg[v] = 0.0f;
+                    if constexpr (A::kBounded) {
+                        TC xr_[2 * R + 1];  // x-neighbours as a row around the point
+                        xr_[R] = q[v][R];
+#pragma unroll
+                        for (int d = 1; d <= R; ++d) {
+                            xr_[R - d] = xn[v][d - 1][0];
+                            xr_[R + d] = xn[v][d - 1][1];
+                        }
+                        sg[v] = sigma_of(star_bound<C>(a, q[v], col + v, xr_ + R));
+                    }
+                }
+#pragma unroll
+                for (int v = 0; v < NPT; ++v) {
+                    A::bfirst(acc[v], sg[v], a, coef_slot<C::SHAPE, R>(0, 0, 0), q[v][R]);
+                    A::centre(acc[v], a, 0, q[v][R]);
+                }
+#pragma unroll
+                for (int d = 1; d <= R; ++d)
+#pragma unroll
+                    for (int v = 0; v < NPT; ++v) {
+                        A::badd(acc[v], sg[v], a, coef_slot<C::SHAPE, R>(-d, 0, 0), q[v][R - d]);
+                        A::badd(acc[v], sg[v], a, coef_slot<C::SHAPE, R>(d, 0, 0), q[v][R + d]);
+                    }
+                if constexpr (!IS2D) {
+#pragma unroll
                     for (int d = 1; d <= R; ++d)
 #pragma unroll
-                        for (int v = 0; v < NPT; ++v) {
-                            const TC *row = pl + own + v * PSTEP;
-                            A::add(acc[v], a, coef_slot<C::SHAPE, R>(0, 0, -d), row[-d]);
-                            A::add(acc[v], a, coef_slot<C::SHAPE, R>(0, 0, d), row[d]);
+                        for (int v = 0; v < VY; ++v) {
+                            A::badd(acc[v], sg[v], a, coef_slot<C::SHAPE, R>(0, -d, 0), col[v + R - d]);
+                            A::badd(acc[v], sg[v], a, coef_slot<C::SHAPE, R>(0, d, 0), col[v + R + d]);
                         }
                 }
+#pragma unroll
+                for (int d = 1; d <= R; ++d)
+#pragma unroll
+                    for (int v = 0; v < NPT; ++v) {
+                        A::badd(acc[v], sg[v], a, coef_slot<C::SHAPE, R>(0, 0, -d), xn[v][d - 1][0]);
+                        A::badd(acc[v], sg[v], a, coef_slot<C::SHAPE, R>(0, 0, d), xn[v][d - 1][1]);
+                    }
             } else {
 #pragma unroll
                 for (int dz = -R; dz <= R; ++dz) {

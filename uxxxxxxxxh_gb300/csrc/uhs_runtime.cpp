@@ -558,7 +558,8 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
     // tile_z overrides it.
     if (!is2d) {
         const bool df = arith == UHS_ARITH_DF32, f32 = sp.dtype == UHS_F32 && !df;
-        if (shape == kStar3) pl->zcap = df ? (R >= 2 ? 64 : 0) : f32 ? (R == 3 ? 64 : 16) : 0;
+        // (float-pair 3d1r star with bounded sums: 374 vs 363 GStencil/s at 16 planes)
+        if (shape == kStar3) pl->zcap = df ? (R >= 2 ? 64 : 16) : f32 ? (R == 3 ? 64 : 16) : 0;
         else if (sep) pl->zcap = (df || f32) ? (R >= 2 ? 64 : f32 ? 16 : 0) : 0;
         else pl->zcap = df ? (R >= 2 ? 16 : 64) : f32 ? (R >= 2 ? 64 : 0) : 0;
     }
