@@ -227,8 +227,8 @@ namespace uhs {
 //
 // The bound's exponent is clamped so sigma stays a normal float (inputs
 // beyond 2^125 overflow the grid: the range flag catches them).
-__device__ __forceinline__ float bound_add(float b, float ch, float2 x) {
-    return __fmaf_rn(fabsf(ch), fabsf(x.x), b);
+__device__ __forceinline__ float bound_add(float b, float cabs, float2 x) {  // cabs = |ch|
+    return __fmaf_rn(cabs, fabsf(x.x), b);
 }
 __device__ __forceinline__ float sigma_of(float b) {
     const float bb = __fmul_ru(b, 1.0000152587890625f);  // 1 + 2^-16

@@ -195,6 +195,7 @@ void batch_fill_args(BatchArgs *a, const StreamCall &c, int nt) {
     a->pair_shift = c.pair_shift;
     a->err = c.err;
     fill_coefs(a->cd, a->chl, a->cl_sum, c.coef, nt < kBatchNT ? nt : kBatchNT, c.shape, c.R);
+    fill_coef_abs(a->cab, a->chl, nt < kBatchNT ? nt : kBatchNT);
 }
 
 }  // namespace uhs

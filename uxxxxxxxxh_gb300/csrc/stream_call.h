@@ -45,6 +45,9 @@ struct StreamArgs {
     // per pass (sep: z, y, x; otherwise [0]); applied once per point to the
     // centre value so the sweep keeps the FP64 coefficients' sum.
     float cl_sum[3];
+    // |ch| of each coefficient: the float-pair bounded sums' bound (df32.cuh
+    // bound_add) reads it as an operand instead of holding |ch| in registers
+    float cab[NT];
 };
 
 // Coefficients in the three forms the kernels use, plus the per-pass sums of
@@ -61,6 +64,9 @@ inline void fill_coefs(double *cd, float2 *chl, float *cl_sum, const double *coe
         sums[pass < 3 ? pass : 2] += v - static_cast<double>(h);
     }
     for (int i = 0; i < 3; ++i) cl_sum[i] = static_cast<float>(sums[i]);
+}
+inline void fill_coef_abs(float *cab, const float2 *chl, int nt) {
+    for (int k = 0; k < nt; ++k) cab[k] = chl[k].x < 0.0f ? -chl[k].x : chl[k].x;
 }
 
 // Everything one streaming launch needs (filled by the runtime).

@@ -229,6 +229,18 @@ __device__ __forceinline__ float2 coef_f2(const Args &a, int k) {
     }
 }
 
+// |ch| of coefficient k (the bounded sums' bound)
+template <class C, class Args>
+__device__ __forceinline__ float coef_abs(const Args &a, int k) {
+    if constexpr (std::is_same_v<Args, BatchArgs>) {
+        float v;
+        asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"((unsigned)__cvta_generic_to_shared(&a.cab[k])));
+        return v;
+    } else {
+        return a.cab[k];
+    }
+}
+
 template <class C, int AR = C::AR>
 struct Arith;
 
@@ -338,28 +350,33 @@ struct Arith<C, kArDf32> {
 
 // Bound B of a star point's bounded sum (df32.cuh): sum |ch_k| |xh_k| over
 // its inputs in the sum's order -- centre, +-d along z, y (rank 3), x.
-// zq: the point's z-queue (centre at [R]); col: its y column (centre at
-// [R]); row: its row in shared memory (centre at [0]).
+// zq: the point's z-queue (centre at [R]); cell: the point's own cell in
+// the staged centre plane (y-neighbours W apart, x-neighbours adjacent).
+// The sums that follow read the same cells; the code generator keeps the
+// loaded values in registers between the two (a warp barrier between them
+// forces reloads and cuts the 3D 13-point float-pair sweep from 118 to 72
+// registers per thread, but measured 4 % slower: 208 against 217 GStencil/s
+// per sweep at 512^3).
 template <class C, class Args, class TC>
-__device__ __forceinline__ float star_bound(const Args &a, const TC *zq, const TC *col, const TC *row) {
-    constexpr int R = C::R;
-    float b = bound_add(0.0f, coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, 0, 0)).x, zq[R]);
+__device__ __forceinline__ float star_bound(const Args &a, const TC *zq, const TC *cell) {
+    constexpr int R = C::R, W = C::W;
+    float b = bound_add(0.0f, coef_abs<C>(a, coef_slot<C::SHAPE, R>(0, 0, 0)), zq[R]);
 #pragma unroll
     for (int d = 1; d <= R; ++d) {
-        b = bound_add(b, coef_f2<C>(a, coef_slot<C::SHAPE, R>(-d, 0, 0)).x, zq[R - d]);
-        b = bound_add(b, coef_f2<C>(a, coef_slot<C::SHAPE, R>(d, 0, 0)).x, zq[R + d]);
+        b = bound_add(b, coef_abs<C>(a, coef_slot<C::SHAPE, R>(-d, 0, 0)), zq[R - d]);
+        b = bound_add(b, coef_abs<C>(a, coef_slot<C::SHAPE, R>(d, 0, 0)), zq[R + d]);
     }
     if constexpr (!C::SI::is2d) {
 #pragma unroll
         for (int d = 1; d <= R; ++d) {
-            b = bound_add(b, coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, -d, 0)).x, col[R - d]);
-            b = bound_add(b, coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, d, 0)).x, col[R + d]);
+            b = bound_add(b, coef_abs<C>(a, coef_slot<C::SHAPE, R>(0, -d, 0)), cell[-d * W]);
+            b = bound_add(b, coef_abs<C>(a, coef_slot<C::SHAPE, R>(0, d, 0)), cell[d * W]);
         }
     }
 #pragma unroll
     for (int d = 1; d <= R; ++d) {
-        b = bound_add(b, coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, 0, -d)).x, row[-d]);
-        b = bound_add(b, coef_f2<C>(a, coef_slot<C::SHAPE, R>(0, 0, d)).x, row[d]);
+        b = bound_add(b, coef_abs<C>(a, coef_slot<C::SHAPE, R>(0, 0, -d)), cell[-d]);
+        b = bound_add(b, coef_abs<C>(a, coef_slot<C::SHAPE, R>(0, 0, d)), cell[d]);
     }
     return b;
 }
@@ -610,7 +627,7 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                 float b0 = 0.0f, b1 = 0.0f;
 #pragma unroll
                 for (int dx = -R; dx <= R; ++dx) {
-                    const float ch = coef_f2<C>(a, CX0 + dx + R).x;
+                    const float ch = coef_abs<C>(a, CX0 + dx + R);
                     b0 = bound_add(b0, ch, r0[dx]);
                     b1 = bound_add(b1, ch, r1[dx]);
                 }
@@ -638,7 +655,7 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                 float b0 = 0.0f, b1 = 0.0f;
 #pragma unroll
                 for (int dy = -R; dy <= R; ++dy) {
-                    const float ch = coef_f2<C>(a, D + dy + R).x;
+                    const float ch = coef_abs<C>(a, D + dy + R);
                     b0 = bound_add(b0, ch, xr[v + R + dy]);
                     b1 = bound_add(b1, ch, xr[v + 1 + R + dy]);
                 }
@@ -671,7 +688,7 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                 if constexpr (A::kBounded) {
                     float b = 0.0f;
 #pragma unroll
-                    for (int dx = -R; dx <= R; ++dx) b = bound_add(b, coef_f2<C>(a, CX0 + dx + R).x, row[dx]);
+                    for (int dx = -R; dx <= R; ++dx) b = bound_add(b, coef_abs<C>(a, CX0 + dx + R), row[dx]);
                     sg = sigma_of(b);
                 }
                 Acc t;
@@ -692,7 +709,7 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                     if constexpr (A::kBounded) {
                         float b = 0.0f;
 #pragma unroll
-                        for (int dy = -R; dy <= R; ++dy) b = bound_add(b, coef_f2<C>(a, D + dy + R).x, xr[v + R + dy]);
+                        for (int dy = -R; dy <= R; ++dy) b = bound_add(b, coef_abs<C>(a, D + dy + R), xr[v + R + dy]);
                         sg = sigma_of(b);
                     }
                     Acc t;
@@ -724,7 +741,7 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                         float b0 = 0.0f, b1 = 0.0f;
 #pragma unroll
                         for (int dz = 0; dz < 2 * R + 1; ++dz) {
-                            const float ch = coef_f2<C>(a, dz).x;
+                            const float ch = coef_abs<C>(a, dz);
                             b0 = bound_add(b0, ch, q[2 * p][dz]);
                             b1 = bound_add(b1, ch, q[2 * p + 1][dz]);
                         }
@@ -740,12 +757,7 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                 } else if constexpr (STAR) {
                     const int sl = slot_j >= R ? slot_j - R : slot_j - R + NRING;
                     const TC *pl = cmp_base + sl * CMP_STRIDE;
-                    // the y column (rank 3) and each point's sigma from all its inputs
-                    TC col[IS2D ? 1 : VY + 2 * R];
-                    if constexpr (!IS2D) {
-#pragma unroll
-                        for (int i = 0; i < VY + 2 * R; ++i) col[i] = pl[own + (i - R) * W];
-                    }
+                    // each point's sigma from all its inputs
                     u64 sg[NPR];
 #pragma unroll
                     for (int p = 0; p < NPR; ++p) {
@@ -753,8 +765,7 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
 #pragma unroll
                         for (int h = 0; h < 2; ++h) {
                             const int v = 2 * p + h;
-                            const TC *row = pl + own + v * PSTEP;
-                            b[h] = star_bound<C>(a, q[v], col + v, row);
+                            b[h] = star_bound<C>(a, q[v], pl + own + v * PSTEP);
                         }
                         sg[p] = pk2(sigma_of(b[0]), sigma_of(b[1]));
                     }
@@ -773,6 +784,9 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                             dfs2_fma_s(acc[p], sg[p], cp.x, cp.y, q[2 * p][R + d], q[2 * p + 1][R + d]);
                         }
                     if constexpr (!IS2D) {
+                        TC col[VY + 2 * R];
+#pragma unroll
+                        for (int i = 0; i < VY + 2 * R; ++i) col[i] = pl[own + (i - R) * W];
 #pragma unroll
                         for (int d = 1; d <= R; ++d)
 #pragma unroll
@@ -855,7 +869,7 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                     if constexpr (A::kBounded) {
                         float b = 0.0f;
 #pragma unroll
-                        for (int dz = 0; dz < 2 * R + 1; ++dz) b = bound_add(b, coef_f2<C>(a, dz).x, q[v][dz]);
+                        for (int dz = 0; dz < 2 * R + 1; ++dz) b = bound_add(b, coef_abs<C>(a, dz), q[v][dz]);
                         sg = sigma_of(b);
                     }
                     A::bfirst(acc[v], sg, a, 0, q[v][0]);
@@ -866,54 +880,12 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
             } else if constexpr (STAR) {
                 const int sl = slot_j >= R ? slot_j - R : slot_j - R + NRING;
                 const TC *pl = cmp_base + sl * CMP_STRIDE;
-                // every input of each point first: the y column (rank 3) and
-                // the x-neighbours, xn[v][d - 1] = {x - d, x + d}
-                TC col[IS2D ? 1 : VY + 2 * R];
-                if constexpr (!IS2D) {
-#pragma unroll
-                    for (int i = 0; i < VY + 2 * R; ++i) col[i] = pl[own + (i - R) * W];
-                }
-                TC xn[NPT][R][2];
-                if constexpr (IS2D && C::XS) {
-                    // x-neighbours from the lanes d columns away (the warp's
-                    // lanes hold consecutive columns; their centre values are
-                    // in the z-queue), the warp's edge lanes from shared memory
-                    const int lane = tid & 31;
-                    const TC cen = q[0][R];
-                    const TC *row = pl + own;
-#pragma unroll
-                    for (int d = 1; d <= R; ++d) {
-                        TC lft = shfl_up_tc(cen, d), rgt = shfl_down_tc(cen, d);
-                        if (lane < d) lft = row[-d];
-                        if (lane >= 32 - d) rgt = row[d];
-                        xn[0][d - 1][0] = lft;
-                        xn[0][d - 1][1] = rgt;
-                    }
-                } else {
-#pragma unroll
-                    for (int v = 0; v < NPT; ++v) {
-                        const TC *row = pl + own + v * PSTEP;
-#pragma unroll
-                        for (int d = 1; d <= R; ++d) {
-                            xn[v][d - 1][0] = row[-d];
-                            xn[v][d - 1][1] = row[d];
-                        }
-                    }
-                }
+                // each point's sigma from all its inputs (float pairs)
                 float sg[NPT];
 #pragma unroll
                 for (int v = 0; v < NPT; ++v) {
                     sg[v] = 0.0f;
-                    if constexpr (A::kBounded) {
-                        TC xr_[2 * R + 1];  // x-neighbours as a row around the point
-                        xr_[R] = q[v][R];
-#pragma unroll
-                        for (int d = 1; d <= R; ++d) {
-                            xr_[R - d] = xn[v][d - 1][0];
-                            xr_[R + d] = xn[v][d - 1][1];
-                        }
-                        sg[v] = sigma_of(star_bound<C>(a, q[v], col + v, xr_ + R));
-                    }
+                    if constexpr (A::kBounded) sg[v] = sigma_of(star_bound<C>(a, q[v], pl + own + v * PSTEP));
                 }
 #pragma unroll
                 for (int v = 0; v < NPT; ++v) {
@@ -928,6 +900,9 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                         A::badd(acc[v], sg[v], a, coef_slot<C::SHAPE, R>(d, 0, 0), q[v][R + d]);
                     }
                 if constexpr (!IS2D) {
+                    TC col[VY + 2 * R];
+#pragma unroll
+                    for (int i = 0; i < VY + 2 * R; ++i) col[i] = pl[own + (i - R) * W];
 #pragma unroll
                     for (int d = 1; d <= R; ++d)
 #pragma unroll
@@ -936,13 +911,31 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
                             A::badd(acc[v], sg[v], a, coef_slot<C::SHAPE, R>(0, d, 0), col[v + R + d]);
                         }
                 }
+                if constexpr (IS2D && C::XS) {
+                    // x-neighbours from the lanes d columns away (the warp's
+                    // lanes hold consecutive columns; their centre values are
+                    // in the z-queue), the warp's edge lanes from shared memory
+                    const int lane = tid & 31;
+                    const TC cen = q[0][R];
+                    const TC *row = pl + own;
 #pragma unroll
-                for (int d = 1; d <= R; ++d)
-#pragma unroll
-                    for (int v = 0; v < NPT; ++v) {
-                        A::badd(acc[v], sg[v], a, coef_slot<C::SHAPE, R>(0, 0, -d), xn[v][d - 1][0]);
-                        A::badd(acc[v], sg[v], a, coef_slot<C::SHAPE, R>(0, 0, d), xn[v][d - 1][1]);
+                    for (int d = 1; d <= R; ++d) {
+                        TC lft = shfl_up_tc(cen, d), rgt = shfl_down_tc(cen, d);
+                        if (lane < d) lft = row[-d];
+                        if (lane >= 32 - d) rgt = row[d];
+                        A::badd(acc[0], sg[0], a, coef_slot<C::SHAPE, R>(0, 0, -d), lft);
+                        A::badd(acc[0], sg[0], a, coef_slot<C::SHAPE, R>(0, 0, d), rgt);
                     }
+                } else {
+#pragma unroll
+                    for (int d = 1; d <= R; ++d)
+#pragma unroll
+                        for (int v = 0; v < NPT; ++v) {
+                            const TC *row = pl + own + v * PSTEP;
+                            A::badd(acc[v], sg[v], a, coef_slot<C::SHAPE, R>(0, 0, -d), row[-d]);
+                            A::badd(acc[v], sg[v], a, coef_slot<C::SHAPE, R>(0, 0, d), row[d]);
+                        }
+                }
             } else {
 #pragma unroll
                 for (int dz = -R; dz <= R; ++dz) {

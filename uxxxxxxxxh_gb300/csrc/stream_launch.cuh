@@ -36,6 +36,7 @@ cudaError_t launch_cfg(const StreamCall &c) {
     a.xoff = C::VX == 2 ? c.xoff : 0;
     a.err = c.err;
     fill_coefs(a.cd, a.chl, a.cl_sum, c.coef, C::NT, c.shape, c.R);
+    fill_coef_abs(a.cab, a.chl, C::NT);
     const int64_t nz = c.ub[0] - c.lb[0], ny = c.ub[1] - c.lb[1], nx = c.ub[2] - c.lb[2];
     if (!c.occ_out && (nz <= 0 || ny <= 0 || nx <= 0)) return cudaSuccess;
     void (*kern)(const StreamArgs<C::NT>);
