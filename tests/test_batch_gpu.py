@@ -143,29 +143,17 @@ def test_large_float_pair_grid_runs_pair_resident_in_the_batch(cuda):
     batch.close()
 
 
-def _separable_box(r, interior, T):
-    from uxxxxxxxxh_gb300.stencil import box_offsets, make_stencil
-    w = [1.0 + abs(d) + 0.1 * d for d in range(-r, r + 1)]
-    offs = box_offsets(3, r)
-    coefs = [w[dz + r] * w[dy + r] * w[dx + r] / sum(w) ** 3 for dz, dy, dx in offs]
-    return make_stencil(f"sep{r}", 3, interior, r, offs, coefs, iterations=T)
-
-
-@pytest.mark.parametrize("case", ["star1", "star2", "star3", "sep1", "sep2"])
-def test_batched_float_pair_sums_match_the_standalone_sweep_bitwise(cuda, case):
+@pytest.mark.parametrize("rank,r", [(3, 1), (3, 2), (3, 3), (2, 1), (2, 2), (2, 3)])
+def test_batched_float_pair_sums_match_the_standalone_sweep_bitwise(cuda, rank, r):
     """The persistent batch kernel sums each point on its own; the standalone
-    3D sweep sums two points per packed instruction.  The float-pair bounded
-    sums (and the separable passes') do the same operations per point in both,
-    so a small FP64 grid in a batch and the same grid swept alone (both in
-    place, T = 4) end with the same bits."""
+    sweep sums two points per packed instruction (rows in 3D, columns in 2D).
+    The float-pair bounded sums do the same operations per point in both, so
+    a small FP64 star in a batch and the same grid swept alone (both in
+    place, T = 4) end with the same bits.  (Boxes are not compared: the
+    batch sweeps them term by term, the standalone plan as separable
+    passes.)"""
     import torch
-    kind, r = case[:-1], int(case[-1])
-    if kind == "star":
-        st, a0 = random_case(3, r, "star", (18, 22, 40), 4, 700 + r)
-    else:
-        st = _separable_box(r, (18, 22, 40), 4)
-        a0 = 2.0 * uhs.workloads.splitmix_uniform(710 + r, int(np.prod(st.sizes))) - 1.0
-        assert uhs.plan(st).factored == 1
+    st, a0 = random_case(rank, r, "star", (18, 22, 40) if rank == 3 else (60, 300), 4, 700 + 10 * rank + r)
     sa = to_dev(a0, st)
     sb = sa.clone()
     uhs.run(st, sa, sb)
