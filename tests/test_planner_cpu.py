@@ -26,7 +26,7 @@ def separable_box(r, dtype):
     return make_stencil(f"sep{r}", 3, (96, 96, 96), r, offs, coefs, dtype=dtype)
 
 
-@pytest.mark.parametrize("r,want", [(1, (64, 8, 2)), (2, (32, 16, 4)), (3, (32, 16, 4))])
+@pytest.mark.parametrize("r,want", [(1, (32, 16, 4)), (2, (32, 16, 4)), (3, (32, 16, 4))])
 def test_float_pair_stars(r, want):
     st, _ = random_case(3, r, "star", (64, 64, 64), 2, 1)
     assert planned(st) == want
@@ -70,15 +70,19 @@ def test_fp32_separable_box_and_2d_strips():
     for r, kind in ((1, "star"), (3, "box")):
         st, _ = random_case(2, r, kind, (300, 700), 2, 5, dtype=F.UHS_F32)
         assert planned(st)[0] == 256
+        # FP64 grids in float pairs: boxes 128-wide strips; stars swept in
+        # place two points per thread over 256 columns (cp.async)
         st64 = st.with_(dtype=F.UHS_F64)
-        assert planned(st64)[0] == 128
+        p = plan(st64, memref_raw(1 << 20, st64.sizes), params=NO_DB)
+        assert (p.tile_x, p.vx) == ((256, 2) if kind == "star" else (128, 1))
 
 
 def test_float_pair_2d_term_by_term_boxes_load_by_cp_async():
     st, _ = random_case(2, 2, "box", (300, 700), 2, 6)
     p = plan(st, memref_raw(1 << 20, st.sizes), params=NO_DB)
     assert p.use_tma == -1
-    star, _ = random_case(2, 2, "star", (300, 700), 2, 6)
+    # stars on float-pair grids take TMA (128 columns, two points per thread)
+    star, _ = random_case(2, 2, "star", (300, 700), 2, 6, dtype=F.UHS_F32X2)
     assert plan(star, memref_raw(1 << 20, star.sizes), params=NO_DB).use_tma == 1
 
 

@@ -486,7 +486,10 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
         // slower).
         if (cfg.tile_x == 0 && p->vx == 0 && shape == kStar2 && !(p->flags & UHS_FLAG_XSHUFFLE)) {
             const bool tma = tma_aligned && cfg.use_tma >= 0;
-            if (arith == UHS_ARITH_DF32) tile = tma ? 3 : 4;
+            // (FP64 grids swept in place, bounded sums, at 8192^2: 256 columns
+            // by cp.async 229 / 194 GStencil/s for r1 / r2 against 217 / 190
+            // at 128 by TMA)
+            if (arith == UHS_ARITH_DF32) tile = (tma && sp.dtype == UHS_F32X2) ? 3 : 4;
             else if (sp.dtype == UHS_F32 && R == 2 && tma) tile = 3;
         }
     } else if (cfg.tile_x == 0 && cfg.tile_y == 0 && p->vy == 0) {
@@ -503,7 +506,9 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
             // 189 vs 191); 3d2r/3d3r stars 186/134 vs 181/127 at 64 x 8;
             // separable boxes r1/r2/r3 235/125/79 (FP64 in place 163/102/68)
             // vs 231/122/76 (162/98/60) at 32 x 32
-            if (shape == kStar3) tile = (R >= 2 || sp.dtype == UHS_F32X2) ? 1 : 2;
+            // (with bounded sums FP64 grids swept in place prefer it too:
+            // 3d1r star 190 vs 177 GStencil/s at 64 x 8)
+            if (shape == kStar3) tile = 1;
             else tile = 1;  // separable and term-by-term boxes (3d1r box 81.6 vs 75.9 at 32 x 32)
         } else if (sp.dtype == UHS_F32) {
             // 3d1r/2r/3r 632/659/438 vs 596/625/410; 32-row tiles for r2 only
@@ -559,7 +564,8 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
     if (!is2d) {
         const bool df = arith == UHS_ARITH_DF32, f32 = sp.dtype == UHS_F32 && !df;
         // (float-pair 3d1r star with bounded sums: 374 vs 363 GStencil/s at 16 planes)
-        if (shape == kStar3) pl->zcap = df ? (R >= 2 ? 64 : 16) : f32 ? (R == 3 ? 64 : 16) : 0;
+        // (FP64 grids swept in place: 64 planes)
+        if (shape == kStar3) pl->zcap = df ? ((R >= 2 || sp.dtype == UHS_F64) ? 64 : 16) : f32 ? (R == 3 ? 64 : 16) : 0;
         else if (sep) pl->zcap = (df || f32) ? (R >= 2 ? 64 : f32 ? 16 : 0) : 0;
         else pl->zcap = df ? (R >= 2 ? 16 : 64) : f32 ? (R >= 2 ? 64 : 0) : 0;
     }
