@@ -488,8 +488,11 @@ static int plan_sweep(const SweepSpec &sp, const uhs_params *p, const GridView &
             const bool tma = tma_aligned && cfg.use_tma >= 0;
             // (FP64 grids swept in place, bounded sums, at 8192^2: 256 columns
             // by cp.async 229 / 194 GStencil/s for r1 / r2 against 217 / 190
-            // at 128 by TMA)
-            if (arith == UHS_ARITH_DF32) tile = (tma && sp.dtype == UHS_F32X2) ? 3 : 4;
+            // at 128 by TMA; radius 3 one point per thread, 129 vs 122)
+            if (arith == UHS_ARITH_DF32) {
+                if (sp.dtype == UHS_F32X2 || cfg.use_tma > 0) tile = tma ? 3 : 4;
+                else tile = R == 3 ? 2 : 4;
+            }
             else if (sp.dtype == UHS_F32 && R == 2 && tma) tile = 3;
         }
     } else if (cfg.tile_x == 0 && cfg.tile_y == 0 && p->vy == 0) {
