@@ -4,7 +4,7 @@
  *   - every partial sum of the extracted high parts (tau) is exact in a float,
  *   - the final pair (after one TwoSum) is within n^2 2^-46 B of the exact
  *     sum, B = sum |ch_k| |xh_k|  (the bound the design states),
- * against sums in __float128.  Prints the largest error / B seen and exits
+ * against sums in binary128.  Prints the largest error / B seen and exits
  * non-zero on a violation.
  *
  * Usage: bounded_sum_check <trials> <seed>
@@ -15,6 +15,13 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+
+/* a binary128 type: long double on AArch64, __float128 on x86-64 */
+#if defined(__aarch64__)
+typedef long double quad;
+#else
+typedef __float128 quad;
+#endif
 
 static uint64_t rng_state;
 static uint64_t next_u64(void) { /* SplitMix64 */
@@ -92,13 +99,13 @@ int main(int argc, char **argv) {
         const float s = tau + lo, v = s - tau;
         const float e = (tau - (s - v)) + (lo - v);
         /* exact value of sum (ch + cl)(xh + xl) */
-        __float128 ex = 0;
+        quad ex = 0;
         for (int k = 0; k < n; ++k)
-            ex += ((__float128)ch[k] + (__float128)cl[k]) * ((__float128)xh[k] + (__float128)xl[k]);
-        const __float128 got = (__float128)s + (__float128)e;
-        __float128 err = got - ex;
+            ex += ((quad)ch[k] + (quad)cl[k]) * ((quad)xh[k] + (quad)xl[k]);
+        const quad got = (quad)s + (quad)e;
+        quad err = got - ex;
         if (err < 0) err = -err;
-        const double rel = b > 0 ? (double)(err / (__float128)b) : 0.0;
+        const double rel = b > 0 ? (double)(err / (quad)b) : 0.0;
         const double bound = (double)n * n * ldexp(1.0, -46);
         if (rel > worst[si]) worst[si] = rel;
         if (rel > bound) {
