@@ -99,10 +99,12 @@ struct StreamCfg {
     static constexpr int SMEM = NSTG * STG_SLOT + (CONVERT ? NCMP * CMP_SLOT : 0) + NSTG * 8;
     static constexpr int THREADS = BX * TYT;
     static constexpr int NT = SI::NT;
-    // 3D sweeps in float-pair arithmetic sum a thread's points two rows at a
-    // time in packed FP32 instructions (df2_*_s, df32.cuh) in standalone
-    // launches.  GB300 at 512^3 (256^3 for radius 2-3 boxes), GStencil/s per
-    // sweep, scalar -> packed: stars on float-pair grids r1/r2/r3 330/184/129
+    // Float-pair sweeps sum a thread's points two at a time in packed FP32
+    // instructions in standalone launches: rows 2p, 2p+1 in 3D, the two
+    // columns of a rank-2 thread with VX = 2 (dfs2_*_s for stars and
+    // separable passes, df2_*_s for term-by-term boxes, df32.cuh).  GB300 at
+    // 512^3 (256^3 for radius 2-3 boxes), GStencil/s per sweep, scalar ->
+    // packed (with TwoSum sums; bounded sums came after): stars on float-pair grids r1/r2/r3 330/184/129
     // -> 341/186/134 (best tiles), on FP64 grids 169/114/86 -> 191/130/97;
     // separable boxes FP64 141/92/63 -> 163/102/68; radius-3 boxes 5.5/6.0 ->
     // 7.5/7.2.  Term-by-term boxes of radius 1 on float-pair grids (100 ->
@@ -539,9 +541,10 @@ __device__ __forceinline__ bool stream_item(const Args &a, int bxi, int byi, int
     const int64_t ostep = VX == 2 ? 1 : a.out_s1;
     constexpr bool SEP = C::SI::sep;
     TC q[NPT][(STAR || SEP) ? 2 * R + 1 : 1];  // z-queue, q[v][R + dz]: star: raw values; sep: xy-filtered
-    // Float-pair 3D sweeps (standalone launches): a thread's points are
-    // summed two rows at a time (2p, 2p+1) into packed accumulators, acc[p]
-    // of df2 (df2_fma_s in df32.cuh).
+    // Float-pair sweeps (standalone launches): a thread's points are
+    // summed two at a time (rows 2p, 2p+1, or a rank-2 thread's two columns)
+    // into packed accumulators, acc[p] of df2 (dfs2_fma_s / df2_fma_s in
+    // df32.cuh).
     constexpr bool PACK = C::PACKED && !std::is_same_v<Args, BatchArgs>;
     constexpr int NPR = PACK ? NPT / 2 : 1;
     unsigned range_err = 0;
