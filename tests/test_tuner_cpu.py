@@ -105,3 +105,31 @@ def test_tuner_skips_a_candidate_that_fails_to_launch(monkeypatch):
     best, results = tuner.Tuner().tune(st, a=object(), b=object(), push=False)
     assert len(results) == len(cands) - 1
     assert best == cands[1]
+
+
+def test_tuner_database_keeps_two_points_along_x_and_reads_version_1(tmp_path):
+    """Files are written as version 2 with the vx column; an entry with two
+    points per thread along x survives a round trip, and a version-1 file
+    (no vx column) still loads, its entries with vx 0 (the planner's
+    choice)."""
+    from uxxxxxxxxh_gb300 import tuner
+    from uxxxxxxxxh_gb300.runtime import RunParams
+    tuner.db_clear()
+    st, _ = random_case(2, 1, "star", (300, 700), 2, 5, dtype=_lib.UHS_F32)
+    tuner.push_params(st, RunParams(kernel=_lib.UHS_KERNEL_STREAM, arith=_lib.UHS_ARITH_FMA, tile_x=128, vx=2), 500.0)
+    path = tmp_path / "tune.db"
+    tuner.db_save(str(path))
+    assert path.read_text().startswith("uhs-tune 2\n")
+    tuner.db_clear()
+    tuner.db_load(str(path))
+    got, exact = tuner.db_get(st)
+    assert exact and (got.tile_x, got.vx) == (128, 2)
+    tuner.db_clear()
+    old = tmp_path / "old.db"
+    old.write_text("uhs-tune 1\n3 0 1 0 64 64 64 2 3 64 8 16 1 1 0 2 0 12.5\n")
+    tuner.db_load(str(old))
+    assert _lib.lib().uhs_tune_size() == 1
+    st3, _ = random_case(3, 1, "star", (64, 64, 64), 2, 5)
+    got, _ = tuner.db_get(st3)
+    assert got is not None and got.vx == 0 and got.tile_x == 64
+    tuner.db_clear()
